@@ -1,0 +1,431 @@
+#!/usr/bin/env python
+"""Benchmark of the KPM hot path: Chebyshev moments of an ELL Hamiltonian.
+
+Workload (default, one GPU): nearest-neighbour graphene on 2048 x 2048
+primitive cells (8,388,608 sites), t = -2.7 eV, Anderson disorder W = 1 eV
+(W(2U-1), seed 1234), ELL width 4 (on-site + 3 bonds), spectrum rescaled by
+the Gershgorin bound x 1.01, M = 2048 moments for R = 8 random-phase vectors
+advanced together, complex128.  A step is one full recursion (all M moments
+for the R vectors): N * R * (M - 1) site-steps.  Inputs are device-resident
+in the timed region and larger than L2 (one vector set is 1.07 GB).
+
+Reported on one JSON line: site-steps/s (value), the roofline of the
+dominant kernel (the fused Chebyshev step) against measured HBM bandwidth,
+its FP64 ceiling (measured live), an end-to-end figure through the
+reference-facing host-pointer call, the CPU baseline (jclsquant's own
+kernels, compiled from its sources, or the C restatement), and SM clocks
+sampled during the timed region.
+
+--impl reference times jclsquant's CPU path on the host cores instead.
+Multi-GPU (torchrun): replicas, each rank runs its own R vectors on the same
+lattice (weak scaling), no data-path collective.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "site-steps/s & HBM GB/s: batched c64 vs plain c128 KPM at ≤1e-6 DOS error"
+UNIT = "site-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=2048, help="lattice side in primitive cells")
+    ap.add_argument("--M", type=int, default=2048)
+    ap.add_argument("--R", type=int, default=8)
+    ap.add_argument("--W", type=float, default=1.0)
+    ap.add_argument("--dtype", default="c128", choices=["c128", "c64"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-clocks", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample length")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def build_problem(cells, W, seed=1234):
+    from minijclsquant_gb300 import lattice
+    from minijclsquant_gb300.ell_matrix import gershgorin_bounds_ell
+    from minijclsquant_gb300.modifiers import modifier_bounds
+
+    arr = lattice.honeycomb_arrays(cells, cells, t=-2.7, W=W, seed=seed, with_geometry=False)
+    bounds = gershgorin_bounds_ell(arr["data"], arr["indices"], arr["n"], factor=1.01)
+
+    class _H:
+        pass
+
+    H = _H()
+    H.data, H.indices, H.bounds = arr["data"], arr["indices"], bounds
+    H.valid_row_values, H.len_row, H.shape = arr["valid"], arr["len_row"], (arr["n"], arr["n"])
+    data_kpm = modifier_bounds(H)
+    return dict(n=arr["n"], L=arr["len_row"], data_kpm=np.ascontiguousarray(data_kpm),
+                indices=np.ascontiguousarray(arr["indices"]), bounds=bounds)
+
+
+def random_vectors(n, R, seed0):
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    return np.stack([random_vector_generator(n, seed0 + r) for r in range(R)])
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index, enabled=True):
+        self.enabled = enabled
+        self.idx = device_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        if not self.enabled:
+            return self
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.enabled or self.proc is None or not self.path:
+            return None
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, fl in rows for i, f in enumerate(fl) if f.lower().startswith("active")})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference_kernels():
+    """jclsquant's own aAxby / vdot compiled from its .pyx (oracle/_ref), or None."""
+    try:
+        from oracle import build as ob
+
+        built = ob.build_reference(names=("blas_funs",))
+        path = built.get("blas_funs")
+        if not path:
+            return None
+        import importlib.util
+
+        spec = importlib.util.spec_from_file_location("blas_funs", path)
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        return mod
+    except Exception:
+        return None
+
+
+def cpu_rec_A_tab(M, prob, v, threads):
+    """One CPU recursion of M moments; returns (seconds, kind)."""
+    blas = cpu_reference_kernels()
+    n, L = prob["n"], prob["L"]
+    if blas is not None:
+        # the loop of jclsquant/recurrence_functions.py:9-40 over jclsquant's own kernels
+        data, idx = prob["data_kpm"], prob["indices"]
+        t0 = time.perf_counter()
+        A_vec = np.zeros(M, dtype=np.complex128)
+        T0 = np.copy(v)
+        T1 = np.zeros(n, dtype=np.complex128)
+        blas.aAxby(1 + 0j, 0 + 0j, v, T1, data, idx, L, n, threads)
+        A_vec[0] = blas.vdot(1 + 0j, v, v, n, threads)
+        A_vec[1] = blas.vdot(1 + 0j, v, T1, n, threads)
+        for m in range(2, M):
+            blas.aAxby(2.0 + 0j, -1 + 0j, T1, T0, data, idx, L, n, threads)
+            T0, T1 = T1, T0
+            A_vec[m] = blas.vdot(1 + 0j, v, T1, n, threads)
+        return time.perf_counter() - t0, "reference"
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    oracle.rec_A_tab(M, prob["data_kpm"], prob["indices"], L, v, threads=threads)
+    return time.perf_counter() - t0, "port"
+
+
+def cpu_baseline(prob, target_s):
+    threads = os.cpu_count() or 1
+    v = random_vectors(prob["n"], 1, 1000)[0]
+    dt, kind = cpu_rec_A_tab(4, prob, v, threads)  # calibration (also warms caches)
+    per_step = max(dt / 3, 1e-6)
+    M = int(min(512, max(8, target_s / per_step)))
+    dt, kind = cpu_rec_A_tab(M, prob, v, threads)
+    steps = prob["n"] * (M - 1)
+    return {"value": steps / dt, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "rec_A_tab loop, 1 vector, M=%d on the full %d-site operator (%d site-steps in %.2f s)"
+                      % (M, prob["n"], steps, dt)}
+
+
+# ---------------------------------------------------------------------------
+def dist_init():
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload_desc(a, n):
+    return ("plain %s KPM moments: honeycomb %dx%d cells (%d sites), t=-2.7 eV, W=%g eV, ELL width 4, "
+            "M=%d, R=%d vectors per launch" % (a.dtype, a.cells, a.cells, n, a.W, a.M, a.R))
+
+
+def run_reference_arm(a):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    prob = build_problem(a.cells, a.W)
+    threads = os.cpu_count() or 1
+    v = random_vectors(prob["n"], 1, 1000)[0]
+    dt, kind = cpu_rec_A_tab(4, prob, v, threads)
+    per_step = max(dt / 3, 1e-6)
+    M = int(min(256, max(8, 10.0 / per_step)))
+    for _ in range(a.warmup):
+        cpu_rec_A_tab(M, prob, v, threads)
+    times = []
+    for _ in range(a.steps):
+        dt, kind = cpu_rec_A_tab(M, prob, v, threads)
+        times.append(dt)
+    tot = sum(times)
+    value = prob["n"] * (M - 1) * a.steps / tot
+    sample = ("each step: rec_A_tab loop (aAxby + vdot per order), 1 vector, M=%d on the full %d-site operator"
+              % (M, prob["n"]))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference",
+            "config": {"workload": workload_desc(a, prob["n"]), "sites": prob["n"], "M": a.M, "R": a.R},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def launches_per_recursion(M, R):
+    groups = []
+    r = R
+    while r > 0:
+        g = 8 if r >= 8 else 4 if r >= 4 else 2 if r >= 2 else 1
+        groups.append(g)
+        r -= g
+    per_group = 2 + 1 + max(0, M - 2) + ((M - 1) // 128 if M > 128 else 0) + 1
+    return per_group * len(groups)
+
+
+def load_traffic(kernel_tag):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", kernel_tag + ".md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def run_ours(a):
+    import ctypes
+
+    import torch
+
+    from minijclsquant_gb300 import _capi, device, obv_gpu
+
+    world, rank, local = dist_init()
+    _capi.load(build_if_missing=False)
+    prob = build_problem(a.cells, a.W)
+    n, L, M, R = prob["n"], prob["L"], a.M, a.R
+    op = device.DeviceELL(prob["data_kpm"], prob["indices"], L)
+    vs_host = random_vectors(n, R, 1000 + rank * R)
+    v = torch.from_numpy(vs_host).cuda()
+    op.reserve(a.dtype, R, M)
+    lib = _capi.lib()
+    stream = torch.cuda.current_stream()
+
+    def step():
+        return device.cheb_moments(op, M, v, dtype=a.dtype)
+
+    for _ in range(a.warmup):
+        mu = step()
+    torch.cuda.synchronize()
+    # timed region
+    lib.kpm_ell_profile(op.handle, 1)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local, enabled=not a.no_clocks) as clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(a.steps):
+            mu = step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier(world)
+    ms = e0.elapsed_time(e1)
+    loop_ms = ctypes.c_double()
+    launches = ctypes.c_int64()
+    rows = ctypes.c_int64()
+    _capi.check(lib.kpm_ell_profile_read(op.handle, ctypes.byref(loop_ms), ctypes.byref(launches), ctypes.byref(rows)))
+    lib.kpm_ell_profile(op.handle, 0)
+    ms_max = max_over_ranks(ms, world)
+    site_steps = float(n) * R * (M - 1) * a.steps
+    value = site_steps * world / (ms_max * 1e-3)
+
+    # sanity: mu_0 = N for unit-modulus vectors
+    mu_h = mu.cpu().numpy()
+    assert np.allclose(mu_h[:, 0].real, n, rtol=1e-6), "moment check failed"
+
+    # roofline of the dominant kernel (the fused step, MODE_NEXT)
+    s_v = 16 if a.dtype == "c128" else 8
+    val_bytes = (8 if op.is_real else 16) if a.dtype == "c128" else (4 if op.is_real else 8)
+    bytes_per_row = L * (val_bytes + 4) + R * 4 * s_v
+    bytes_per_launch = float(n) * bytes_per_row
+    avg_launch_s = (loop_ms.value * 1e-3) / max(1, launches.value)
+    achieved_gbs = bytes_per_launch / avg_launch_s / 1e9
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    hbm_peak = peaks.get("hbm_gbs")
+    peak_src = "MEASURED_PEAKS.json hbm_gbs (measured)"
+    if not hbm_peak:
+        hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
+    tag = "cheb_step_%s_r%d_%dx%d" % (a.dtype, R, a.cells, a.cells)
+    traffic = load_traffic(tag)
+    roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
+                "kernel": "cheb_step_kernel (MODE_NEXT, STORE|MOM1)",
+                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
+    fma_rate = ctypes.c_double()
+    _capi.check(lib.kpm_measure_fp64_fma_rate(ctypes.byref(fma_rate), ctypes.c_void_p(int(stream.cuda_stream))))
+    fma_per_site_step = (2 * L if op.is_real else 4 * L) + 4
+    fp64 = None
+    if a.dtype == "c128":
+        ach = fma_per_site_step * float(n) * R / avg_launch_s
+        fp64 = {"achieved_fma_per_s": ach, "peak_fma_per_s": fma_rate.value, "frac": ach / fma_rate.value,
+                "fma_per_site_step": fma_per_site_step, "peak_source": "measured live (independent FP64 FMA chains)"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+            "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if a.dtype == "c128" else "f32 (f64 moment accumulation)", "data": "synthetic",
+            "config": {"workload": workload_desc(a, n), "sites": n, "M": M, "R": R, "len_row": L, "W": a.W,
+                       "bounds": "Gershgorin x 1.01", "l2": "inputs larger than L2 (vector set %.2f GB)"
+                       % (n * R * s_v / 1e9), "parallelism": "replicas x%d" % world},
+            "roofline": roofline, "fp64": fp64, "gpu_launches": launches_per_recursion(M, R) * a.steps,
+            "hbm_gbs": achieved_gbs}
+    if clk.summary() is not None:
+        line["clocks"] = clk.summary()
+
+    # end to end through the reference-facing host-pointer call (rec_A_tab_gpu per vector, as
+    # jclsquant's kpm_dos_gpu issues it): operator and vector uploads inside the timed region.
+    if not a.no_e2e and a.dtype == "c128":
+        data_p = torch.from_numpy(prob["data_kpm"]).pin_memory().numpy()
+        idx_p = torch.from_numpy(prob["indices"]).pin_memory().numpy()
+        vs_p = torch.from_numpy(vs_host).pin_memory().numpy()
+        out = torch.zeros((R, M), dtype=torch.complex128).pin_memory().numpy()
+        obv_gpu.rec_A_tab_gpu(data_p, idx_p, L, np.ascontiguousarray(vs_p[0]), out[0], M)  # warm-up
+        torch.cuda.synchronize()
+        barrier(world)
+        t0 = time.perf_counter()
+        e2e_steps = 1
+        for _ in range(e2e_steps):
+            for r in range(R):
+                obv_gpu.rec_A_tab_gpu(data_p, idx_p, L, vs_p[r], out[r], M)
+        torch.cuda.synchronize()
+        dt = max_over_ranks(time.perf_counter() - t0, world)
+        assert np.allclose(out[:, 0].real, n, rtol=1e-6)
+        line["e2e"] = {"value": float(n) * R * (M - 1) * e2e_steps * world / dt, "unit": UNIT,
+                       "h2d_bytes_per_step": int(R * (prob["data_kpm"].nbytes + prob["indices"].nbytes + n * 16)),
+                       "d2h_bytes_per_step": int(R * M * 16),
+                       "path": "obv_gpu.rec_A_tab_gpu -> exported rec_A_tab (host pointers, one vector per call)"}
+    if rank == 0 and world == 1 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(prob, a.cpu_seconds)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference_arm(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,166 @@
+/*
+ * kpm.h -- C ABI of libkpm, the sm_103a Kernel Polynomial Method hot path.
+ *
+ * The library holds an ELL Hamiltonian on one GPU and runs the fused
+ * "ELL SpMV + three-term Chebyshev recursion + moment reduction" on it:
+ *
+ *     T_0 = v,  T_1 = H v,  T_{m+1} = 2 H T_m - T_{m-1},
+ *     mu_m = <v_l | T_m>   (conjugate on the left vector)
+ *
+ * where H is the already-rescaled operator (spectrum inside [-1, 1]).
+ *
+ * Conventions
+ *  - Every entry point returns an int status (KPM_OK == 0); kpm_strerror()
+ *    names it.  The reference-compatible entry points at the end return void,
+ *    exactly like the functions they replace; their status is read with
+ *    kpm_last_status().
+ *  - Complex numbers are interleaved (re, im) doubles: a "c128 array of n"
+ *    is 2n doubles.  Sets of R vectors are passed vector-major: [R][n].
+ *  - Pointers marked "device" must be CUDA device (or managed) memory; the
+ *    caller owns every buffer it passes.  Operators (kpm_ell) own their
+ *    device storage and a reusable workspace.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  Calls are
+ *    stream-ordered; they return once the work is enqueued unless stated.
+ *  - One handle may be used by one host thread at a time; distinct handles
+ *    are independent.
+ */
+#ifndef KPM_GB300_H
+#define KPM_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define KPM_OK 0
+#define KPM_ERR_INVALID_ARG 1   /* null pointer, non-positive size, bad flag  */
+#define KPM_ERR_SHAPE 2         /* sizes that do not match the operator       */
+#define KPM_ERR_DTYPE 3         /* unknown precision selector                 */
+#define KPM_ERR_OOM 4           /* device allocation failed                   */
+#define KPM_ERR_CUDA 5          /* a CUDA runtime call or launch failed       */
+#define KPM_ERR_TIMEOUT 6       /* a bounded device-side wait gave up         */
+#define KPM_ERR_INDEX 7         /* an ELL column index is outside [0, n)      */
+#define KPM_ERR_UNSUPPORTED 8   /* valid request this build does not serve    */
+#define KPM_ERR_NONFINITE 9     /* a moment came out NaN or Inf               */
+
+/* ---- precision selectors ----------------------------------------------- */
+#define KPM_C128 0   /* complex128 recursion, FP64 moments (the drop-in form)   */
+#define KPM_C64 1    /* complex64 recursion and values, FP64 moment accumulation */
+
+/* ---- operator creation flags ------------------------------------------- */
+#define KPM_FLAG_DEVICE_PTRS 1u   /* data/indices are device pointers        */
+#define KPM_FLAG_SPLIT_DIAG 2u    /* store slots with col == row separately   */
+
+typedef struct kpm_ell_s kpm_ell;
+
+const char* kpm_strerror(int status);
+/* Library version as major*10000 + minor*100 + patch. */
+int kpm_version(void);
+
+/*
+ * Create a device-resident operator from the reference's padded row-major
+ * (AoS) ELL arrays: data[i*len_row + j] (c128) and indices[i*len_row + j]
+ * (int32), the layout built by jclsquant's data_indices_c
+ * (jclsquant/cython_modules/Extra_funs.pyx:81-137) and consumed by
+ * aAxby_c (jclsquant/cython_modules/blas_funs.pyx:64-71).  Padding slots
+ * (value 0) are kept; column indices are validated (KPM_ERR_INDEX).
+ * The values are stored as given (no rescaling): pass H~ = H / a, as the
+ * reference passes H_kpm.data to rec_A_tab_gpu (jclsquant/observables_gpu.py:37).
+ * When every value has a zero imaginary part the operator stores real values
+ * (half the bytes, half the FP64 work); results are unchanged.
+ * Replaces the per-call uploads of jclsquant/cuda_cython/cuda/recursions.cu:24-28.
+ */
+int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* data,
+                   const int32_t* indices, unsigned flags, void* stream);
+int kpm_ell_destroy(kpm_ell* h);
+/* Query: n_rows, len_row, 1 if values are stored real, device bytes held. */
+int kpm_ell_info(const kpm_ell* h, int64_t* n_rows, int* len_row, int* is_real,
+                 int64_t* device_bytes);
+/* Pre-size the workspace for (dtype, R) so later calls allocate nothing. */
+int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M);
+
+/*
+ * y <- b*y + a*H x on R vectors ([R][n] c128, device).
+ * Replaces ell_matrix.dot (jclsquant/ell_matrix.py:209-211) ->
+ * aAxby (jclsquant/cython_modules/blas_funs.pyx:64-71).
+ */
+int kpm_ell_dot(kpm_ell* h, double a_re, double a_im, double b_re, double b_im,
+                const double* x, double* y, int R, void* stream);
+
+/*
+ * Chebyshev moments for R vector pairs, m = 0..M-1:
+ *   mu[r][m]    = <v_l[r] | T_m(H) v_r[r]>        (v_l == NULL: v_l = v_r)
+ *   mu_rr[r][m] = <v_r[r] | T_m(H) v_r[r]>        (optional, may be NULL)
+ * v_r, v_l: device [R][n] c128.  mu, mu_rr: device [R][M] c128.
+ * dtype KPM_C128 is the drop-in form; KPM_C64 runs the recursion in
+ * complex64 and accumulates moments in FP64.
+ * Replaces rec_A_tab (jclsquant/recurrence_functions.py:9-40;
+ * jclsquant/cuda_cython/cuda/recursions.cu:17-98), rec_A_tab2v
+ * (recurrence_functions.py:44-74; recursions.cu:180-263) and
+ * rec_A_tab2v_2 (recurrence_functions.py:76-111), for R vectors per call.
+ */
+int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r,
+                     const double* v_l, double* mu, double* mu_rr, void* stream);
+
+/*
+ * out[r] = sum_{m<M} c[m] T_m(H) v[r]   (c: device [M] c128; v, out: device [R][n] c128;
+ * out may alias v).  Replaces rec_A_vec (jclsquant/recurrence_functions.py:114-143)
+ * and the device rec_A (jclsquant/cuda_cython/cuda/recursions.cu:267-317).
+ */
+int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const double* v,
+                    double* out, void* stream);
+
+/*
+ * Commutator series out[r] = sum_m c[m] C_m with C_0 = 0, C_1 = V v,
+ * C_m = 2 H C_{m-1} - C_{m-2} + 2 V T_{m-1}.  H and V are separate operators
+ * of equal size.  Replaces rec_com_A_vec (jclsquant/recurrence_functions.py:146-196;
+ * jclsquant/cuda_cython/cuda/recursions.cu:319-388).
+ */
+int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M,
+                               const double* c, const double* v, double* out, void* stream);
+
+/*
+ * Time-domain Kubo correlator sigma[r][j] = <U_c(t_j) | V1 U(t_j)>, j < len_t,
+ * with U(t_0) = v, U_c(t_0) = sum_m c_fd[m] C_m (commutator series with V2),
+ * and both advanced per time step by the series with c_u (M2 terms).
+ * The caller multiplies by -i as jclsquant/observables_gpu.py does.
+ * c_u: device [M2] c128; c_fd: device [M] c128; v: device [R][n]; sigma: device [R][len_t].
+ * Replaces for_time_sigma (jclsquant/cuda_cython/cuda/obv.cu:124-176).
+ */
+int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u,
+                   int M2, const double* c_fd, int M, int len_t, const double* v,
+                   double* sigma, void* stream);
+
+/* ---- reference-compatible host-pointer entry points ---------------------
+ * Same names and argument lists as jclsquant/cuda_cython/cuda/obv.h:21-23,30,
+ * where std::complex<double>* is passed as double* (identical layout).
+ * Host buffers in and out; synchronous; the operator is uploaded per call,
+ * as in the reference.  Status: kpm_last_status() (per host thread).
+ */
+void rec_A_tab(double* data, int* indices, int len_row, int N, double* A_vec, double* v, int M);
+void rec_A_tab_2(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l,
+                 double* v_r, int M);
+void for_time_sigma(double* data, double* data2, double* data3, int* indices, int len_row, int N,
+                    double* moments_kernel_U, double* moments_kernel_FD, int len_t,
+                    double* sigma_vec, double* v, int M, int M2);
+int kpm_last_status(void);
+
+/* ---- measurement hooks (no counterpart in the reference) ----------------
+ * kpm_ell_profile(h, 1) starts recording CUDA events around every recursion
+ * step loop run on h (on the call's stream); kpm_ell_profile_read()
+ * synchronises on them and returns the summed loop time, the number of step
+ * launches timed and the rows each launch covers.  kpm_ell_profile(h, 0)
+ * stops recording and drops what was recorded.
+ * kpm_measure_fp64_fma_rate() times a kernel of independent FP64 FMA chains
+ * on every SM and returns FMA/s (the FP64 ceiling of the complex128 path). */
+int kpm_ell_profile(kpm_ell* h, int enable);
+int kpm_ell_profile_read(kpm_ell* h, double* loop_ms, int64_t* step_launches, int64_t* rows_per_launch);
+int kpm_measure_fp64_fma_rate(double* fma_per_second, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KPM_GB300_H */

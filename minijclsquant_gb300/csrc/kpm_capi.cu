@@ -1,0 +1,529 @@
+// kpm_capi.cu -- the C ABI declared in include/kpm.h: operator handles, the
+// recursion drivers (moments, series, commutator, time-domain Kubo) and the
+// reference-compatible host-pointer entry points.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "kpm_internal.cuh"
+
+namespace kpm {
+int comm_series_packed(kpm_ell_s* h, kpm_ell_s* v, int Rg, int M, const double2* coef, const double2* x,
+                       double2* result, cudaStream_t s);
+}
+
+using namespace kpm;
+
+namespace {
+
+thread_local int g_last_status = KPM_OK;
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---- ELL ingest -------------------------------------------------------------
+__global__ void ell_validate_kernel(const double2* __restrict__ data, const int32_t* __restrict__ idx, int64_t count,
+                                    int64_t n, unsigned* flags) {
+  unsigned f = 0;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = idx[t];
+    if (c < 0 || (int64_t)c >= n) f |= 1u;
+    if (data[t].y != 0.0) f |= 2u;
+    if (!isfinite(data[t].x) || !isfinite(data[t].y)) f |= 4u;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+// AoS [row][slot] -> SoA [slot][n_pad], values doubled (exact).
+__global__ void ell_repack_kernel(const double2* __restrict__ data, const int32_t* __restrict__ idx, int64_t n,
+                                  int64_t n_pad, int L, bool real, void* val, int32_t* col) {
+  const int64_t total = (int64_t)L * n_pad;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / n_pad);
+    const int64_t row = t % n_pad;
+    double2 v = make_double2(0.0, 0.0);
+    int32_t c = 0;
+    if (row < n) {
+      const int64_t src = row * L + s;
+      v = data[src];
+      c = idx[src];
+    }
+    col[t] = c;
+    if (real)
+      static_cast<double*>(val)[t] = 2.0 * v.x;
+    else
+      static_cast<double2*>(val)[t] = make_double2(2.0 * v.x, 2.0 * v.y);
+  }
+}
+
+int grid_1d(int64_t total) {
+  int64_t g = (total + 255) / 256;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(g, 65536));
+}
+
+int pow2_group(int remaining) {
+  if (remaining >= 8) return 8;
+  if (remaining >= 4) return 4;
+  if (remaining >= 2) return 2;
+  return 1;
+}
+
+int vpt_for(bool f32, int Rg) { return (f32 && Rg >= 2) ? 2 : 1; }
+
+StepParams base_params(kpm_ell_s* h, bool f32) {
+  StepParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.val = f32 ? h->val32 : h->val64;
+  p.col = h->col;
+  p.ld = h->n_pad;
+  p.L = h->L;
+  p.n_pad = h->n_pad;
+  p.a_half = make_double2(0.5, 0.0);
+  p.b = make_double2(0.0, 0.0);
+  return p;
+}
+
+int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s) {
+  return f32 ? launch_step_f32(real, R, mode, epi, p, grid, s) : launch_step_f64(real, R, mode, epi, p, grid, s);
+}
+
+// Moments for one group of Rg <= 8 vectors starting at r0.
+int moments_group(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const double* v_r, const double* v_l,
+                  double* mu, double* mu_rr, cudaStream_t s) {
+  const int vpt = vpt_for(f32, Rg);
+  const int grid = grid_for(h, Rg, vpt);
+  const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+  const int sets = mu_rr ? 2 : 1;
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  if (sets == 2) KPM_TRY(ensure(ws.vr, vb));
+  const int64_t step_stride = (int64_t)sets * grid * Rg;
+  KPM_TRY(ensure(ws.part, (size_t)kChunk * step_stride * sizeof(double2)));
+  KPM_TRY(pack_vectors(v_r, h->n, h->n_pad, R, r0, Rg, f32, ws.ta.p, s));
+  KPM_TRY(pack_vectors(v_l ? v_l : v_r, h->n, h->n_pad, R, r0, Rg, f32, ws.vl.p, s));
+  if (sets == 2) KPM_TRY(pack_vectors(v_r, h->n, h->n_pad, R, r0, Rg, f32, ws.vr.p, s));
+
+  double2* part = static_cast<double2*>(ws.part.p);
+  double* outs[2] = {mu, mu_rr};
+  StepParams p = base_params(h, f32);
+  p.vl = ws.vl.p;
+  p.vl2 = sets == 2 ? ws.vr.p : nullptr;
+  p.part_step_stride = step_stride;
+  // m = 1 (and the moment of T_0)
+  p.tcur = ws.ta.p;
+  p.tout = ws.tb.p;
+  p.part = part;
+  KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_FIRST, EPI_STORE | EPI_MOM1, p, grid, s));
+  void* tprev = ws.ta.p;  // T_{m-2}
+  void* tcur = ws.tb.p;   // T_{m-1}
+  int m0 = 0;
+  cudaEvent_t ev = nullptr;
+  if (M > 2) KPM_TRY(prof_begin(h, s, &ev));
+  for (int m = 2; m < M; ++m) {
+    if (m - m0 == kChunk) {
+      KPM_TRY(reduce_partials(part, kChunk, sets, grid, Rg, outs, R, r0, M, m0, s));
+      m0 = m;
+    }
+    p.tcur = tcur;
+    p.tout = tprev;
+    p.part = part + (int64_t)(m - m0) * step_stride;
+    KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_NEXT, EPI_STORE | EPI_MOM1, p, grid, s));
+    std::swap(tprev, tcur);
+  }
+  if (M > 2) KPM_TRY(prof_end(h, s, ev, M - 2));
+  KPM_TRY(reduce_partials(part, M - m0, sets, grid, Rg, outs, R, r0, M, m0, s));
+  return KPM_OK;
+}
+
+// Series on one packed group: x ([n_pad][Rg], working precision) -> result (same layout).
+int series_packed(kpm_ell_s* h, bool f32, int Rg, int M, const double2* coef, const void* x, void* result,
+                  cudaStream_t s) {
+  const int vpt = vpt_for(f32, Rg);
+  const int grid = grid_for(h, Rg, vpt);
+  const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+  KPM_TRY(ensure(h->ws.ta, vb));
+  KPM_TRY(ensure(h->ws.tb, vb));
+  KPM_CUDA_TRY(cudaMemcpyAsync(h->ws.ta.p, x, vb, cudaMemcpyDeviceToDevice, s));
+  StepParams p = base_params(h, f32);
+  p.series = result;
+  p.coef = coef;
+  p.tcur = h->ws.ta.p;
+  p.tout = h->ws.tb.p;
+  p.m = 1;
+  KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_FIRST, EPI_STORE | EPI_SERIES, p, grid, s));
+  void* tprev = h->ws.ta.p;
+  void* tcur = h->ws.tb.p;
+  for (int m = 2; m < M; ++m) {
+    p.tcur = tcur;
+    p.tout = tprev;
+    p.m = m;
+    KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_NEXT, EPI_STORE | EPI_SERIES, p, grid, s));
+    std::swap(tprev, tcur);
+  }
+  return KPM_OK;
+}
+
+int check_dtype(int dtype) { return (dtype == KPM_C128 || dtype == KPM_C64) ? KPM_OK : KPM_ERR_DTYPE; }
+
+}  // namespace
+
+extern "C" {
+
+const char* kpm_strerror(int status) {
+  switch (status) {
+    case KPM_OK: return "ok";
+    case KPM_ERR_INVALID_ARG: return "invalid argument";
+    case KPM_ERR_SHAPE: return "shape mismatch";
+    case KPM_ERR_DTYPE: return "unknown dtype";
+    case KPM_ERR_OOM: return "device out of memory";
+    case KPM_ERR_CUDA: return "CUDA error";
+    case KPM_ERR_TIMEOUT: return "device-side wait timed out";
+    case KPM_ERR_INDEX: return "ELL column index out of range";
+    case KPM_ERR_UNSUPPORTED: return "unsupported request";
+    case KPM_ERR_NONFINITE: return "non-finite value";
+    default: return "unknown status";
+  }
+}
+
+int kpm_version(void) { return 100; }
+
+int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* data, const int32_t* indices,
+                   unsigned flags, void* stream) {
+  if (!out || !data || !indices || n_rows < 1 || len_row < 1) return KPM_ERR_INVALID_ARG;
+  if (n_rows > (int64_t)INT32_MAX) return KPM_ERR_SHAPE;
+  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG)) return KPM_ERR_INVALID_ARG;
+  *out = nullptr;
+  cudaStream_t s = as_stream(stream);
+  kpm_ell_s* h = new kpm_ell_s();
+  h->n = n_rows;
+  h->L = len_row;
+  h->n_pad = ((n_rows + kRowAlign - 1) / kRowAlign) * kRowAlign;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    delete h;
+    return KPM_ERR_CUDA;
+  }
+  h->device = dev;
+  const int64_t count = n_rows * (int64_t)len_row;
+  const double2* d_data = reinterpret_cast<const double2*>(data);
+  const int32_t* d_idx = indices;
+  DevBuf stage_data, stage_idx, flag_buf;
+  int st = KPM_OK;
+  auto fail = [&](int code) {
+    release(stage_data);
+    release(stage_idx);
+    release(flag_buf);
+    kpm_ell_destroy(h);
+    return code;
+  };
+  if (!(flags & KPM_FLAG_DEVICE_PTRS)) {
+    if ((st = ensure(stage_data, count * sizeof(double2))) != KPM_OK) return fail(st);
+    if ((st = ensure(stage_idx, count * sizeof(int32_t))) != KPM_OK) return fail(st);
+    e = cudaMemcpyAsync(stage_data.p, data, count * sizeof(double2), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(stage_idx.p, indices, count * sizeof(int32_t), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      return fail(KPM_ERR_CUDA);
+    }
+    d_data = static_cast<const double2*>(stage_data.p);
+    d_idx = static_cast<const int32_t*>(stage_idx.p);
+  }
+  if ((st = ensure(flag_buf, sizeof(unsigned))) != KPM_OK) return fail(st);
+  e = cudaMemsetAsync(flag_buf.p, 0, sizeof(unsigned), s);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return fail(KPM_ERR_CUDA);
+  }
+  ell_validate_kernel<<<grid_1d(count), 256, 0, s>>>(d_data, d_idx, count, n_rows, static_cast<unsigned*>(flag_buf.p));
+  unsigned hflags = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hflags, flag_buf.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return fail(KPM_ERR_CUDA);
+  }
+  if (hflags & 1u) return fail(KPM_ERR_INDEX);
+  if (hflags & 4u) return fail(KPM_ERR_NONFINITE);
+  h->is_real = (hflags & 2u) ? 0 : 1;
+  const int64_t slots = (int64_t)len_row * h->n_pad;
+  e = cudaMalloc(&h->val64, slots * (h->is_real ? sizeof(double) : sizeof(double2)));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->col), slots * sizeof(int32_t));
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    (void)cudaGetLastError();
+    return fail(KPM_ERR_OOM);
+  }
+  ell_repack_kernel<<<grid_1d(slots), 256, 0, s>>>(d_data, d_idx, n_rows, h->n_pad, len_row, h->is_real != 0,
+                                                    h->val64, h->col);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return fail(KPM_ERR_CUDA);
+  }
+  release(stage_data);
+  release(stage_idx);
+  release(flag_buf);
+  *out = h;
+  return KPM_OK;
+}
+
+int kpm_ell_destroy(kpm_ell* h) {
+  if (!h) return KPM_ERR_INVALID_ARG;
+  if (h->val64) cudaFree(h->val64);
+  if (h->val32) cudaFree(h->val32);
+  if (h->col) cudaFree(h->col);
+  Workspace& w = h->ws;
+  DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef};
+  for (DevBuf* b : bufs) release(*b);
+  kpm_ell_profile(h, 0);
+  delete h;
+  return KPM_OK;
+}
+
+int kpm_ell_info(const kpm_ell* h, int64_t* n_rows, int* len_row, int* is_real, int64_t* device_bytes) {
+  if (!h) return KPM_ERR_INVALID_ARG;
+  if (n_rows) *n_rows = h->n;
+  if (len_row) *len_row = h->L;
+  if (is_real) *is_real = h->is_real;
+  if (device_bytes) {
+    int64_t slots = (int64_t)h->L * h->n_pad;
+    int64_t b = slots * (h->is_real ? 8 : 16) + slots * 4;
+    if (h->val32) b += slots * (h->is_real ? 4 : 8);
+    const Workspace& w = h->ws;
+    const DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef};
+    for (const DevBuf* d : bufs) b += (int64_t)d->bytes;
+    *device_bytes = b;
+  }
+  return KPM_OK;
+}
+
+int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M) {
+  if (!h || R < 1 || M < 1) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  const bool f32 = dtype == KPM_C64;
+  if (f32) KPM_TRY(ensure_f32_values(h, 0));
+  const int Rg = pow2_group(R);
+  const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  KPM_TRY(ensure(ws.vr, vb));
+  const int grid = grid_for(h, Rg, vpt_for(f32, Rg));
+  KPM_TRY(ensure(ws.part, (size_t)kChunk * 2 * grid * Rg * sizeof(double2)));
+  KPM_CUDA_TRY(cudaDeviceSynchronize());
+  return KPM_OK;
+}
+
+int kpm_ell_dot(kpm_ell* h, double a_re, double a_im, double b_re, double b_im, const double* x, double* y, int R,
+                void* stream) {
+  if (!h || !x || !y || R < 1) return KPM_ERR_INVALID_ARG;
+  cudaStream_t s = as_stream(stream);
+  for (int r0 = 0; r0 < R; r0 += pow2_group(R - r0)) {
+    const int Rg = pow2_group(R - r0);
+    const size_t vb = (size_t)h->n_pad * Rg * sizeof(double2);
+    KPM_TRY(ensure(h->ws.ta, vb));
+    KPM_TRY(ensure(h->ws.tb, vb));
+    KPM_TRY(pack_vectors(x, h->n, h->n_pad, R, r0, Rg, false, h->ws.ta.p, s));
+    const bool use_b = (b_re != 0.0 || b_im != 0.0);
+    if (use_b) KPM_TRY(pack_vectors(y, h->n, h->n_pad, R, r0, Rg, false, h->ws.tb.p, s));
+    StepParams p = base_params(h, false);
+    p.tcur = h->ws.ta.p;
+    p.tout = h->ws.tb.p;
+    p.a_half = make_double2(0.5 * a_re, 0.5 * a_im);
+    p.b = make_double2(b_re, b_im);
+    KPM_TRY(launch_step(false, h->is_real, Rg, MODE_APPLY, EPI_STORE, p, grid_for(h, Rg, 1), s));
+    KPM_TRY(unpack_vectors(h->ws.tb.p, false, h->n, h->n_pad, R, r0, Rg, y, s));
+  }
+  return KPM_OK;
+}
+
+int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r, const double* v_l, double* mu,
+                     double* mu_rr, void* stream) {
+  if (!h || !v_r || !mu || R < 1 || M < 1) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  const bool f32 = dtype == KPM_C64;
+  cudaStream_t s = as_stream(stream);
+  if (f32) KPM_TRY(ensure_f32_values(h, s));
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = pow2_group(R - r0);
+    KPM_TRY(moments_group(h, f32, R, r0, Rg, M, v_r, v_l, mu, mu_rr, s));
+    r0 += Rg;
+  }
+  return KPM_OK;
+}
+
+int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const double* v, double* out,
+                    void* stream) {
+  if (!h || !c || !v || !out || R < 1 || M < 2) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  const bool f32 = dtype == KPM_C64;
+  cudaStream_t s = as_stream(stream);
+  if (f32) KPM_TRY(ensure_f32_values(h, s));
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = pow2_group(R - r0);
+    const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+    KPM_TRY(ensure(h->ws.tc, vb));
+    KPM_TRY(ensure(h->ws.acc, vb));
+    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, f32, h->ws.tc.p, s));
+    KPM_TRY(series_packed(h, f32, Rg, M, reinterpret_cast<const double2*>(c), h->ws.tc.p, h->ws.acc.p, s));
+    KPM_TRY(unpack_vectors(h->ws.acc.p, f32, h->n, h->n_pad, R, r0, Rg, out, s));
+    r0 += Rg;
+  }
+  return KPM_OK;
+}
+
+int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M, const double* c, const double* v,
+                               double* out, void* stream) {
+  if (!h || !v_op || !c || !v || !out || R < 1 || M < 2) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  if (v_op->n != h->n) return KPM_ERR_SHAPE;
+  if (dtype != KPM_C128) return KPM_ERR_UNSUPPORTED;
+  cudaStream_t s = as_stream(stream);
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = pow2_group(R - r0);
+    const size_t vb = (size_t)h->n_pad * Rg * sizeof(double2);
+    KPM_TRY(ensure(h->ws.vl, vb));
+    KPM_TRY(ensure(h->ws.acc, vb));
+    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, false, h->ws.vl.p, s));
+    KPM_TRY(comm_series_packed(h, v_op, Rg, M, reinterpret_cast<const double2*>(c),
+                               static_cast<const double2*>(h->ws.vl.p), static_cast<double2*>(h->ws.acc.p), s));
+    KPM_TRY(unpack_vectors(h->ws.acc.p, false, h->n, h->n_pad, R, r0, Rg, out, s));
+    r0 += Rg;
+  }
+  return KPM_OK;
+}
+
+int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u, int M2,
+                   const double* c_fd, int M, int len_t, const double* v, double* sigma, void* stream) {
+  if (!h || !v1 || !v2 || !c_u || !c_fd || !v || !sigma || R < 1 || M < 2 || M2 < 2 || len_t < 1)
+    return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  if (dtype != KPM_C128) return KPM_ERR_UNSUPPORTED;
+  if (v1->n != h->n || v2->n != h->n) return KPM_ERR_SHAPE;
+  cudaStream_t s = as_stream(stream);
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = pow2_group(R - r0);
+    const size_t vb = (size_t)h->n_pad * Rg * sizeof(double2);
+    Workspace& ws = h->ws;
+    KPM_TRY(ensure(ws.vl, vb));   // v (input of the commutator series)
+    KPM_TRY(ensure(ws.vr, vb));   // U
+    KPM_TRY(ensure(ws.acc, vb));  // U_c
+    const int grid = grid_for(v1, Rg, 1);
+    KPM_TRY(ensure(ws.part, (size_t)grid * Rg * sizeof(double2)));
+    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, false, ws.vr.p, s));
+    KPM_CUDA_TRY(cudaMemcpyAsync(ws.vl.p, ws.vr.p, vb, cudaMemcpyDeviceToDevice, s));
+    KPM_TRY(comm_series_packed(h, v2, Rg, M, reinterpret_cast<const double2*>(c_fd),
+                               static_cast<const double2*>(ws.vl.p), static_cast<double2*>(ws.acc.p), s));
+    double* outs[2] = {sigma, sigma};
+    for (int j = 0; j < len_t; ++j) {
+      if (j > 0) {
+        KPM_TRY(series_packed(h, false, Rg, M2, reinterpret_cast<const double2*>(c_u), ws.vr.p, ws.vl.p, s));
+        KPM_CUDA_TRY(cudaMemcpyAsync(ws.vr.p, ws.vl.p, vb, cudaMemcpyDeviceToDevice, s));
+        KPM_TRY(series_packed(h, false, Rg, M2, reinterpret_cast<const double2*>(c_u), ws.acc.p, ws.vl.p, s));
+        KPM_CUDA_TRY(cudaMemcpyAsync(ws.acc.p, ws.vl.p, vb, cudaMemcpyDeviceToDevice, s));
+      }
+      // sigma_j = <U_c | V1 U>
+      StepParams p = base_params(v1, false);
+      p.tcur = ws.vr.p;
+      p.vl = ws.acc.p;
+      p.part = static_cast<double2*>(ws.part.p);
+      p.a_half = make_double2(0.5, 0.0);
+      KPM_TRY(launch_step(false, v1->is_real, Rg, MODE_APPLY, EPI_MOM1, p, grid, s));
+      KPM_TRY(reduce_partials(static_cast<double2*>(ws.part.p), 1, 1, grid, Rg, outs, R, r0, len_t, j, s));
+    }
+    r0 += Rg;
+  }
+  return KPM_OK;
+}
+
+int kpm_last_status(void) { return g_last_status; }
+
+// ---- reference-compatible host-pointer entry points -------------------------
+static int host_rec(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l, double* v_r,
+                    int M) {
+  if (!data || !indices || !A_vec || !v_r || N < 1 || len_row < 1 || M < 1) return KPM_ERR_INVALID_ARG;
+  kpm_ell* h = nullptr;
+  KPM_TRY(kpm_ell_create(&h, N, len_row, data, indices, 0u, nullptr));
+  DevBuf dv, dl, dmu;
+  int st = ensure(dv, (size_t)N * sizeof(double2));
+  if (st == KPM_OK && v_l) st = ensure(dl, (size_t)N * sizeof(double2));
+  if (st == KPM_OK) st = ensure(dmu, (size_t)M * sizeof(double2));
+  cudaError_t e = cudaSuccess;
+  if (st == KPM_OK) e = cudaMemcpy(dv.p, v_r, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess && v_l)
+    e = cudaMemcpy(dl.p, v_l, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess)
+    st = kpm_cheb_moments(h, KPM_C128, 1, M, static_cast<double*>(dv.p), v_l ? static_cast<double*>(dl.p) : nullptr,
+                          static_cast<double*>(dmu.p), nullptr, nullptr);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(A_vec, dmu.p, (size_t)M * sizeof(double2), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    st = KPM_ERR_CUDA;
+  }
+  release(dv);
+  release(dl);
+  release(dmu);
+  kpm_ell_destroy(h);
+  return st;
+}
+
+void rec_A_tab(double* data, int* indices, int len_row, int N, double* A_vec, double* v, int M) {
+  g_last_status = host_rec(data, indices, len_row, N, A_vec, nullptr, v, M);
+}
+
+void rec_A_tab_2(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l, double* v_r, int M) {
+  g_last_status = host_rec(data, indices, len_row, N, A_vec, v_l, v_r, M);
+}
+
+void for_time_sigma(double* data, double* data2, double* data3, int* indices, int len_row, int N,
+                    double* moments_kernel_U, double* moments_kernel_FD, int len_t, double* sigma_vec, double* v,
+                    int M, int M2) {
+  int st = KPM_OK;
+  if (!data || !data2 || !data3 || !indices || !moments_kernel_U || !moments_kernel_FD || !sigma_vec || !v || N < 1 ||
+      len_row < 1 || len_t < 1 || M < 2 || M2 < 2) {
+    g_last_status = KPM_ERR_INVALID_ARG;
+    return;
+  }
+  kpm_ell *h = nullptr, *v1 = nullptr, *v2 = nullptr;
+  st = kpm_ell_create(&h, N, len_row, data, indices, 0u, nullptr);
+  if (st == KPM_OK) st = kpm_ell_create(&v1, N, len_row, data2, indices, 0u, nullptr);
+  if (st == KPM_OK) st = kpm_ell_create(&v2, N, len_row, data3, indices, 0u, nullptr);
+  DevBuf dcu, dcf, dv, dsig;
+  if (st == KPM_OK) st = ensure(dcu, (size_t)M2 * sizeof(double2));
+  if (st == KPM_OK) st = ensure(dcf, (size_t)M * sizeof(double2));
+  if (st == KPM_OK) st = ensure(dv, (size_t)N * sizeof(double2));
+  if (st == KPM_OK) st = ensure(dsig, (size_t)len_t * sizeof(double2));
+  cudaError_t e = cudaSuccess;
+  if (st == KPM_OK) e = cudaMemcpy(dcu.p, moments_kernel_U, (size_t)M2 * sizeof(double2), cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess)
+    e = cudaMemcpy(dcf.p, moments_kernel_FD, (size_t)M * sizeof(double2), cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(dv.p, v, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess)
+    st = kpm_time_sigma(h, v1, v2, KPM_C128, 1, static_cast<double*>(dcu.p), M2, static_cast<double*>(dcf.p), M,
+                        len_t, static_cast<double*>(dv.p), static_cast<double*>(dsig.p), nullptr);
+  if (st == KPM_OK && e == cudaSuccess)
+    e = cudaMemcpy(sigma_vec, dsig.p, (size_t)len_t * sizeof(double2), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    st = KPM_ERR_CUDA;
+  }
+  release(dcu);
+  release(dcf);
+  release(dv);
+  release(dsig);
+  if (h) kpm_ell_destroy(h);
+  if (v1) kpm_ell_destroy(v1);
+  if (v2) kpm_ell_destroy(v2);
+  g_last_status = st;
+}
+
+}  // extern "C"

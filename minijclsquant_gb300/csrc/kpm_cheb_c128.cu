@@ -1,0 +1,25 @@
+// Complex128 instantiations of the fused step kernel (the drop-in form).
+#include "kpm_cheb.cuh"
+
+namespace kpm {
+
+int launch_step_f64(bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s) {
+  switch (R) {
+    case 1:
+      return real ? launch_mode_epi<double, true, 1, 1>(mode, epi, p, grid, s)
+                  : launch_mode_epi<double, false, 1, 1>(mode, epi, p, grid, s);
+    case 2:
+      return real ? launch_mode_epi<double, true, 2, 1>(mode, epi, p, grid, s)
+                  : launch_mode_epi<double, false, 2, 1>(mode, epi, p, grid, s);
+    case 4:
+      return real ? launch_mode_epi<double, true, 4, 1>(mode, epi, p, grid, s)
+                  : launch_mode_epi<double, false, 4, 1>(mode, epi, p, grid, s);
+    case 8:
+      return real ? launch_mode_epi<double, true, 8, 1>(mode, epi, p, grid, s)
+                  : launch_mode_epi<double, false, 8, 1>(mode, epi, p, grid, s);
+    default:
+      return KPM_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace kpm

@@ -1,0 +1,27 @@
+// Complex64 instantiations of the fused step kernel (mixed precision: complex64
+// vectors and values, FP64 moment accumulation).  Two complex64 values per
+// thread make every access a 16-byte vector load.
+#include "kpm_cheb.cuh"
+
+namespace kpm {
+
+int launch_step_f32(bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s) {
+  switch (R) {
+    case 1:
+      return real ? launch_mode_epi<float, true, 1, 1>(mode, epi, p, grid, s)
+                  : launch_mode_epi<float, false, 1, 1>(mode, epi, p, grid, s);
+    case 2:
+      return real ? launch_mode_epi<float, true, 1, 2>(mode, epi, p, grid, s)
+                  : launch_mode_epi<float, false, 1, 2>(mode, epi, p, grid, s);
+    case 4:
+      return real ? launch_mode_epi<float, true, 2, 2>(mode, epi, p, grid, s)
+                  : launch_mode_epi<float, false, 2, 2>(mode, epi, p, grid, s);
+    case 8:
+      return real ? launch_mode_epi<float, true, 4, 2>(mode, epi, p, grid, s)
+                  : launch_mode_epi<float, false, 4, 2>(mode, epi, p, grid, s);
+    default:
+      return KPM_ERR_UNSUPPORTED;
+  }
+}
+
+}  // namespace kpm

@@ -1,0 +1,128 @@
+// kpm_internal.cuh -- shared definitions of libkpm (not part of the public ABI).
+//
+// Device layout of an operator (struct kpm_ell_s):
+//   val64 : 2*H values, SoA [slot][n_pad]; double when every value is real,
+//           double2 (re, im) otherwise.  Doubling is exact in binary floating
+//           point, so T_{m+1} = (2H) T_m - T_{m-1} needs no extra multiply.
+//   val32 : the same values rounded to float / float2 (built on first KPM_C64 use)
+//   col   : int32 column indices, SoA [slot][n_pad]
+// Rows are padded to a multiple of kRowAlign with value 0 and column 0, so
+// every kernel runs without a bounds check in its inner loop.
+//
+// Vectors inside the library are "site-major": R vectors of one site are
+// adjacent ([n_pad][R] complex), so the R threads (or R/2 for complex64) that
+// serve one row read one contiguous 16-byte-aligned segment per gathered site.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstddef>
+#include <utility>
+#include <vector>
+
+#include "../../include/kpm.h"
+
+namespace kpm {
+
+constexpr int kBlock = 256;       // threads per CTA of every streaming kernel
+constexpr int kRowAlign = 256;    // n_pad is a multiple of this
+constexpr int kMaxGroupR = 8;     // vectors advanced together by one launch
+constexpr int kChunk = 128;       // recursion steps whose moment partials are buffered
+
+void set_last_cuda_error(cudaError_t e);
+
+#define KPM_CUDA_TRY(expr)                                  \
+  do {                                                      \
+    cudaError_t kpm_e_ = (expr);                            \
+    if (kpm_e_ != cudaSuccess) {                            \
+      ::kpm::set_last_cuda_error(kpm_e_);                   \
+      return kpm_e_ == cudaErrorMemoryAllocation ? KPM_ERR_OOM : KPM_ERR_CUDA; \
+    }                                                       \
+  } while (0)
+
+#define KPM_TRY(expr)            \
+  do {                           \
+    int kpm_s_ = (expr);         \
+    if (kpm_s_ != KPM_OK) return kpm_s_; \
+  } while (0)
+
+// Grow-only device buffer.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+int ensure(DevBuf& b, size_t bytes);
+void release(DevBuf& b);
+
+struct Workspace {
+  DevBuf ta, tb, tc, td;   // recursion vectors
+  DevBuf vl, vr;           // packed left vectors for the moments
+  DevBuf acc, acc2;        // series accumulators
+  DevBuf part;             // per-CTA moment partials [kChunk][sets][grid][R] double2
+  DevBuf coef;             // small device staging (coefficients)
+};
+
+}  // namespace kpm
+
+struct kpm_ell_s {
+  int64_t n = 0;       // rows (= columns)
+  int64_t n_pad = 0;   // padded rows
+  int L = 0;           // ELL slots per row
+  int is_real = 0;     // values stored real
+  int device = 0;
+  void* val64 = nullptr;
+  void* val32 = nullptr;
+  int32_t* col = nullptr;
+  int sm_count = 0;
+  kpm::Workspace ws;
+  // measurement hook state (kpm_ell_profile)
+  int prof = 0;
+  int64_t prof_launches = 0;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
+};
+
+namespace kpm {
+
+// Kernel parameter block of the fused step kernel (kpm_cheb.cuh).
+struct StepParams {
+  const void* val;        // 2H values [L][ld] (T or complex T)
+  const int32_t* col;     // [L][ld]
+  int64_t ld;             // SoA row stride (= n_pad)
+  int L;
+  int64_t n_pad;          // rows to process
+  const void* tcur;       // gathered vector set      [n_pad][R]
+  void* tout;             // NEXT: T_{m-1} in, T_{m+1} out (in place); FIRST/APPLY: output
+  const void* t0;         // FIRST: own-row T_0 for mu_0 (== tcur)
+  const void* vl;         // left vectors for moment set 1 [n_pad][R]
+  const void* vl2;        // left vectors for moment set 2 (or null)
+  double2* part;          // partials for this launch: [sets][grid][R] (FIRST: [2 steps][sets][grid][R])
+  int64_t part_step_stride;  // elements between consecutive steps' partial blocks
+  void* series;           // series accumulator [n_pad][R]
+  const double2* coef;    // series coefficients (device)
+  int m;                  // recursion index of the vector being produced
+  double2 a_half;         // APPLY: a/2 (values are 2H)
+  double2 b;              // APPLY: b
+};
+
+// Launch helpers implemented per precision (kpm_cheb_c128.cu, kpm_cheb_c64.cu).
+enum Mode { MODE_FIRST = 0, MODE_NEXT = 1, MODE_APPLY = 2 };
+enum Epi { EPI_STORE = 1, EPI_MOM1 = 2, EPI_MOM2 = 4, EPI_SERIES = 8, EPI_APPLY_B = 16 };
+
+int launch_step_f64(bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
+int launch_step_f32(bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
+int grid_for(const kpm_ell_s* h, int R, int vpt);
+
+// Layout helpers (kpm_util.cu).
+int pack_vectors(const double* src, int64_t n, int64_t n_pad, int R, int r0, int Rg, bool to_f32,
+                 void* dst, cudaStream_t s);
+int unpack_vectors(const void* src, bool from_f32, int64_t n, int64_t n_pad, int R, int r0, int Rg,
+                   double* dst, cudaStream_t s);
+int reduce_partials(const double2* part, int steps, int sets, int grid, int Rg, double* const* outs,
+                    int R, int r0, int M, int m0, cudaStream_t s);
+int ensure_f32_values(kpm_ell_s* h, cudaStream_t s);
+// Profiling helpers: bracket a step loop with events when h->prof is set.
+int prof_begin(kpm_ell_s* h, cudaStream_t s, cudaEvent_t* ev);
+int prof_end(kpm_ell_s* h, cudaStream_t s, cudaEvent_t ev, int64_t launches);
+
+}  // namespace kpm

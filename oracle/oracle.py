@@ -1,0 +1,146 @@
+"""numpy-facing wrapper of the C oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
+use this module, as the checker (and the CPU baseline "port"); the product
+library never imports it.  Each function follows the reference routine named
+in its docstring (the C file gives file:line for each).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        c = ctypes.CDLL(path)
+        P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+        c.oracle_aAxby.argtypes = [D, D, D, D, P, P, P, P, I, I, I]
+        c.oracle_aAxby.restype = None
+        c.oracle_vdot.argtypes = [D, D, P, P, I, I, P]
+        c.oracle_vdot.restype = None
+        c.oracle_dot.argtypes = [D, D, P, P, I, I, P]
+        c.oracle_dot.restype = None
+        c.oracle_rec_A_tab.argtypes = [I, P, P, I, I, P, P, I]
+        c.oracle_rec_A_tab2v.argtypes = [I, P, P, I, I, P, P, P, I]
+        c.oracle_rec_A_tab2v_2.argtypes = [I, P, P, I, I, P, P, P, P, I]
+        c.oracle_rec_A_vec.argtypes = [I, P, P, I, I, P, P, P, I]
+        c.oracle_rec_com_A_vec.argtypes = [I, P, P, P, I, I, P, P, P, I]
+        c.oracle_for_time_sigma.argtypes = [P, P, P, P, I, I, P, P, I, P, P, I, I, I]
+        c.oracle_max_threads.restype = I
+        _lib = c
+    return _lib
+
+
+def default_threads() -> int:
+    env = os.environ.get("OMP_NUM_THREADS")
+    return int(env) if env else (os.cpu_count() or 1)
+
+
+def _c(a, dtype):
+    return np.ascontiguousarray(np.asarray(a, dtype=dtype))
+
+
+def _check(rc, what):
+    if rc != 0:
+        raise RuntimeError("oracle %s failed (%d)" % (what, rc))
+
+
+def aAxby(a, b, x, y, data, indices, len_row, threads=None):
+    """y <- b*y + a*A x in place (blas_funs.pyx:64-71)."""
+    x = _c(x, np.complex128)
+    assert y.dtype == np.complex128 and y.flags.c_contiguous
+    data, indices = _c(data, np.complex128), _c(indices, np.int32)
+    a, b = complex(a), complex(b)
+    lib().oracle_aAxby(a.real, a.imag, b.real, b.imag, x.ctypes.data, y.ctypes.data, data.ctypes.data,
+                       indices.ctypes.data, int(len_row), y.size, threads or default_threads())
+    return y
+
+
+def vdot(x, y, threads=None):
+    """sum y * conj(x) (blas_funs.pyx:83-88)."""
+    x, y = _c(x, np.complex128), _c(y, np.complex128)
+    out = np.zeros(2)
+    lib().oracle_vdot(1.0, 0.0, x.ctypes.data, y.ctypes.data, x.size, threads or default_threads(), out.ctypes.data)
+    return out[0] + 1j * out[1]
+
+
+def rec_A_tab(M, data, indices, len_row, v, threads=None):
+    """<v|T_m v>, m < M (recurrence_functions.py:9-40)."""
+    data, indices, v = _c(data, np.complex128), _c(indices, np.int32), _c(v, np.complex128)
+    mu = np.zeros(M, dtype=np.complex128)
+    _check(lib().oracle_rec_A_tab(int(M), data.ctypes.data, indices.ctypes.data, int(len_row), v.size, v.ctypes.data,
+                                  mu.ctypes.data, threads or default_threads()), "rec_A_tab")
+    return mu
+
+
+def rec_A_tab2v(M, data, indices, len_row, v_l, v_r, threads=None):
+    """<v_l|T_m v_r> (recurrence_functions.py:44-74)."""
+    data, indices = _c(data, np.complex128), _c(indices, np.int32)
+    v_l, v_r = _c(v_l, np.complex128), _c(v_r, np.complex128)
+    mu = np.zeros(M, dtype=np.complex128)
+    _check(lib().oracle_rec_A_tab2v(int(M), data.ctypes.data, indices.ctypes.data, int(len_row), v_r.size,
+                                    v_l.ctypes.data, v_r.ctypes.data, mu.ctypes.data, threads or default_threads()),
+           "rec_A_tab2v")
+    return mu
+
+
+def rec_A_tab2v_2(M, data, indices, len_row, v_l, v_r, threads=None):
+    """(<v_l|T_m v_r>, <v_r|T_m v_r>) (recurrence_functions.py:76-111)."""
+    data, indices = _c(data, np.complex128), _c(indices, np.int32)
+    v_l, v_r = _c(v_l, np.complex128), _c(v_r, np.complex128)
+    m1 = np.zeros(M, dtype=np.complex128)
+    m2 = np.zeros(M, dtype=np.complex128)
+    _check(lib().oracle_rec_A_tab2v_2(int(M), data.ctypes.data, indices.ctypes.data, int(len_row), v_r.size,
+                                      v_l.ctypes.data, v_r.ctypes.data, m1.ctypes.data, m2.ctypes.data,
+                                      threads or default_threads()), "rec_A_tab2v_2")
+    return m1, m2
+
+
+def rec_A_vec(M, data, indices, len_row, c, v, threads=None):
+    """sum_m c_m T_m v (recurrence_functions.py:114-143)."""
+    data, indices = _c(data, np.complex128), _c(indices, np.int32)
+    c, v = _c(c, np.complex128), _c(v, np.complex128)
+    out = np.zeros_like(v)
+    _check(lib().oracle_rec_A_vec(int(M), data.ctypes.data, indices.ctypes.data, int(len_row), v.size, c.ctypes.data,
+                                  v.ctypes.data, out.ctypes.data, threads or default_threads()), "rec_A_vec")
+    return out
+
+
+def rec_com_A_vec(M, data_a, data_v, indices, len_row, c, v, threads=None):
+    """Commutator series (recurrence_functions.py:146-196); A and V share `indices`."""
+    data_a, data_v = _c(data_a, np.complex128), _c(data_v, np.complex128)
+    indices, c, v = _c(indices, np.int32), _c(c, np.complex128), _c(v, np.complex128)
+    out = np.zeros_like(v)
+    _check(lib().oracle_rec_com_A_vec(int(M), data_a.ctypes.data, data_v.ctypes.data, indices.ctypes.data,
+                                      int(len_row), v.size, c.ctypes.data, v.ctypes.data, out.ctypes.data,
+                                      threads or default_threads()), "rec_com_A_vec")
+    return out
+
+
+def for_time_sigma(data_h, data_v1, data_v2, indices, len_row, c_u, c_fd, len_t, v, M, M2, threads=None):
+    """<U_c(t_j)|V1 U(t_j)> (obv.cu:124-176)."""
+    arrs = [_c(a, np.complex128) for a in (data_h, data_v1, data_v2, c_u, c_fd, v)]
+    indices = _c(indices, np.int32)
+    sig = np.zeros(int(len_t), dtype=np.complex128)
+    _check(lib().oracle_for_time_sigma(arrs[0].ctypes.data, arrs[1].ctypes.data, arrs[2].ctypes.data,
+                                       indices.ctypes.data, int(len_row), arrs[5].size, arrs[3].ctypes.data,
+                                       arrs[4].ctypes.data, int(len_t), sig.ctypes.data, arrs[5].ctypes.data, int(M),
+                                       int(M2), threads or default_threads()), "for_time_sigma")
+    return sig
+
+
+def moment_tolerance_ok(mu, ref, rel=1e-10, floor_frac=1e-6):
+    """Per-order check |mu_m - ref_m| <= rel * max(|ref_m|, floor_frac * |ref_0|)."""
+    mu, ref = np.asarray(mu), np.asarray(ref)
+    scale = np.maximum(np.abs(ref), floor_frac * np.abs(ref[..., :1]))
+    err = np.abs(mu - ref) / scale
+    return bool(np.all(err <= rel)), float(np.max(err))

@@ -1,0 +1,108 @@
+"""The oracle (C restatement of jclsquant's CPU path) pinned against the
+golden vectors produced by the reference itself (tests/golden/make_golden.py).
+CPU only."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden
+from oracle import oracle
+
+CASES = ["honeycomb_8x8", "ref_graphene_256", "complex_open_6x5", "irregular_300"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_moments_match_reference(case):
+    z = golden(case)
+    L = int(z["len_row"])
+    for r in range(z["v"].shape[0]):
+        mu = oracle.rec_A_tab(int(z["M"]), z["data_kpm"], z["indices"], L, z["v"][r])
+        ok, err = oracle.moment_tolerance_ok(mu, z["mu"][r], rel=1e-12)
+        assert ok, (case, r, err)
+
+
+def test_oracle_moments_thread_count_independent():
+    z = golden("irregular_300")
+    L = int(z["len_row"])
+    a = oracle.rec_A_tab(int(z["M"]), z["data_kpm"], z["indices"], L, z["v"][0], threads=1)
+    b = oracle.rec_A_tab(int(z["M"]), z["data_kpm"], z["indices"], L, z["v"][0], threads=4)
+    assert oracle.moment_tolerance_ok(a, b, rel=1e-12)[0]
+
+
+def test_oracle_other_recursions_match_reference():
+    z = golden("honeycomb_8x8")
+    x = golden("honeycomb_8x8_more")
+    L = int(z["len_row"])
+    d, ix, v = z["data_kpm"], z["indices"], z["v"][0]
+    M = int(z["M"])
+    assert oracle.moment_tolerance_ok(oracle.rec_A_tab2v(M, d, ix, L, x["v_l"], v), x["mu_lr"], 1e-12)[0]
+    a, b = oracle.rec_A_tab2v_2(M, d, ix, L, x["v_l"], v)
+    assert oracle.moment_tolerance_ok(a, x["mu2_a"], 1e-12)[0]
+    assert oracle.moment_tolerance_ok(b, x["mu2_b"], 1e-12)[0]
+    Ms = len(x["coef"])
+    s = oracle.rec_A_vec(Ms, d, ix, L, x["coef"], v)
+    assert np.max(np.abs(s - x["series"])) <= 1e-12 * np.max(np.abs(x["series"]))
+    c = oracle.rec_com_A_vec(Ms, d, x["v2_data"], ix, L, x["coef"], v)
+    assert np.max(np.abs(c - x["comm"])) <= 1e-12 * np.max(np.abs(x["comm"]))
+    sig = oracle.for_time_sigma(d, x["v1_data"], x["v2_data"], ix, L, x["cu"], x["coef"], int(x["len_t"]), v, Ms,
+                                int(x["M2"]))
+    assert np.max(np.abs(sig - x["sigma"])) <= 1e-11 * np.max(np.abs(x["sigma"]))
+
+
+def test_oracle_tiny_and_short_recursions():
+    z = golden("tiny_2x2")
+    L = int(z["len_row"])
+    assert np.allclose(oracle.rec_A_tab(2, z["data_kpm"], z["indices"], L, z["v"]), z["mu2"], rtol=1e-14, atol=1e-14)
+    assert np.allclose(oracle.rec_A_tab(3, z["data_kpm"], z["indices"], L, z["v"]), z["mu3"], rtol=1e-14, atol=1e-14)
+    # the reference rejects M = 1 with an IndexError
+    assert str(z["m1_error"]) == "IndexError"
+
+
+def test_oracle_cpu_dos_configuration():
+    """64 x 64 cells (8192 sites), M = 512, 4 vectors: inputs rebuilt by the lattice builder,
+    checked by digest against what the reference was fed, then the oracle against its moments."""
+    from minijclsquant_gb300 import lattice
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from tests.golden.make_golden import digest
+
+    z = golden("honeycomb_64x64")
+    arr = lattice.honeycomb_arrays(64, 64, t=-2.7, W=0.5, seed=1234)
+    from minijclsquant_gb300.ell_matrix import ell_matrix
+
+    H = ell_matrix(lattice.to_csr(arr))
+    assert digest(H.data, H.indices) == str(z["input_digest"])
+    assert np.array_equal(H.bounds, z["bounds"])
+    Hk = H.modifier(modifier_bounds)
+    assert digest(Hk.data) == str(z["kpm_digest"])
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    for r, seed in enumerate(z["seeds"]):
+        v = random_vector_generator(8192, int(seed))
+        mu = oracle.rec_A_tab(int(z["M"]), Hk.data, Hk.indices, int(z["len_row"]), v)
+        # OpenMP combines per-thread partial sums in completion order, so two runs of
+        # the same code differ by up to ~1e-12 per order at M = 512: pin at 1e-11.
+        ok, err = oracle.moment_tolerance_ok(mu, z["mu"][r], rel=1e-11)
+        assert ok, err
+
+
+@pytest.mark.skipif(not os.path.isdir("/root/reference/jclsquant"), reason="reference tree not present")
+def test_oracle_against_live_reference():
+    """Fresh seeded case, run through the live reference (built from its .pyx) and the oracle."""
+    from oracle import reference_import
+
+    ref = reference_import.load()
+    from minijclsquant_gb300 import lattice
+
+    arr = lattice.honeycomb_arrays(5, 7, t=-2.1, W=0.8, seed=4321, periodic=False)
+    H = ref.ell_matrix.ell_matrix(lattice.to_csr(arr))
+    Hk = H.modifier(ref.modifiers.modifier_bounds)
+    v = ref.observables.random_vector_generator(H.shape[0], 99)
+    mu_ref = ref.recurrence_functions.rec_A_tab(40, Hk, v)
+    mu = oracle.rec_A_tab(40, Hk.data, Hk.indices, H.len_row, v)
+    assert oracle.moment_tolerance_ok(mu, mu_ref, 1e-12)[0]
+    y_ref = np.zeros_like(v)
+    y = np.zeros_like(v)
+    ref.blas_funs.aAxby(2 + 0j, -1 + 0j, v, y_ref, Hk.data, Hk.indices, H.len_row, H.shape[0], 2)
+    oracle.aAxby(2, -1, v, y, Hk.data, Hk.indices, H.len_row)
+    assert np.max(np.abs(y - y_ref)) <= 1e-14 * np.max(np.abs(y_ref))

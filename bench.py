@@ -55,6 +55,11 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-clocks", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU-baseline sample length")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched complex64 ensemble measurement")
+    ap.add_argument("--batch-inst", type=int, default=256)
+    ap.add_argument("--batch-M", type=int, default=1024)
+    ap.add_argument("--batch-R", type=int, default=2)
+    ap.add_argument("--batch-side-max", type=int, default=512)
     return ap.parse_args()
 
 
@@ -295,6 +300,66 @@ def load_traffic(kernel_tag):
     return None
 
 
+def run_batched(a, hbm_peak, steps, warmup):
+    """The batched mixed-precision configuration: uneven honeycomb instances (side
+    32..side_max cells, W ~ U[0, 2] eV, own seed each), R vectors per instance, M
+    moments; complex64 recursion with FP64 moment accumulation, timed against the
+    same ensemble in complex128; DOS error of every instance against complex128."""
+    import torch
+
+    from minijclsquant_gb300 import batched
+
+    t0 = time.perf_counter()
+    datas, idxs, L, bnds, prm = batched.honeycomb_ensemble(a.batch_inst, side_range=(32, a.batch_side_max),
+                                                           W_range=(0.0, 2.0), seed=42)
+    B = batched.BatchedELL(datas, idxs, L)
+    setup_s = time.perf_counter() - t0
+    del datas, idxs
+    R, M = a.batch_R, a.batch_M
+    v = torch.from_numpy(batched.ensemble_vectors(B.rows, R)).cuda()
+    stream = torch.cuda.current_stream()
+
+    def timed(dtype, k_steps, w_steps):
+        for _ in range(w_steps):
+            mu = B.moments(M, v, dtype=dtype)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k_steps):
+            mu = B.moments(M, v, dtype=dtype)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return mu, e0.elapsed_time(e1) / k_steps
+
+    mu64, ms64 = timed("c64", steps, warmup)
+    mu128, ms128 = timed("c128", 1, 1)
+    mu64 = mu64.cpu().numpy()
+    mu128 = mu128.cpu().numpy()
+    site_steps = float(B.n_total) * R * (M - 1)
+    val64 = site_steps / (ms64 * 1e-3)
+    val128 = site_steps / (ms128 * 1e-3)
+    d64 = batched.batched_dos(mu64, bnds, M)
+    d128 = batched.batched_dos(mu128, bnds, M)
+    dos_err = max(float(np.max(np.abs(x[:, 1] - y[:, 1])) / np.max(np.abs(y[:, 1]))) for x, y in zip(d64, d128))
+    mom_err = np.abs(mu64 - mu128) / np.abs(mu128[:, :, :1])
+    per_order = mom_err.max(axis=(0, 1))
+    bytes_per_site_step = L * (4 + 4) / R + 4 * 8
+    ach = bytes_per_site_step * val64 / 1e9
+    return {"workload": "%d honeycomb instances, sides U{32..%d} cells (%d sites total), W~U[0,2] eV, R=%d, M=%d"
+                        % (B.n_inst, a.batch_side_max, B.n_total, R, M),
+            "value": val64, "unit": UNIT, "ms_per_step": ms64, "dtype": "c64 recursion, f64 moment accumulation",
+            "hbm_gbs": ach, "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
+                                         "frac": ach / hbm_peak, "bytes_per_site_step": bytes_per_site_step},
+            "c128_same_ensemble": {"value": val128, "ms_per_step": ms128},
+            "speedup_c64_vs_c128": val64 / val128,
+            "dos_error_max_over_instances": dos_err,
+            "moment_error_vs_c128": {"max_rel_mu0": float(per_order.max()),
+                                     "by_order": {str(m): float(per_order[m]) for m in (1, 10, 100, 500, M - 1) if m < M}},
+            "setup_s": setup_s, "graph": "one CUDA graph launch per recursion",
+            "gpu_launches_per_step": 2 + 1 + max(0, M - 2) + 1}
+
+
 def run_ours(a):
     import ctypes
 
@@ -363,9 +428,14 @@ def run_ours(a):
         hbm_peak, peak_src = 6800.0, "fallback 6.8 TB/s"
     tag = "cheb_step_%s_r%d_%dx%d" % (a.dtype, R, a.cells, a.cells)
     traffic = load_traffic(tag)
+    kind, rpt, grid, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+    _capi.check(lib.kpm_ell_step_config(op.handle, _capi.dtype_code(a.dtype), R, ctypes.byref(kind), ctypes.byref(rpt),
+                                        ctypes.byref(grid), ctypes.byref(us)))
+    kname = ("cheb_next_staged_kernel (bulk-copy staged, %d row(s)/thread)" % rpt.value if kind.value == 1
+             else "cheb_step_kernel (grid-stride, MODE_NEXT STORE|MOM1)")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
-                "kernel": "cheb_step_kernel (MODE_NEXT, STORE|MOM1)",
+                "kernel": kname, "grid": grid.value,
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
     fma_rate = ctypes.c_double()
     _capi.check(lib.kpm_measure_fp64_fma_rate(ctypes.byref(fma_rate), ctypes.c_void_p(int(stream.cuda_stream))))
@@ -384,8 +454,9 @@ def run_ours(a):
                        % (n * R * s_v / 1e9), "parallelism": "replicas x%d" % world},
             "roofline": roofline, "fp64": fp64, "gpu_launches": launches_per_recursion(M, R) * a.steps,
             "hbm_gbs": achieved_gbs}
-    if clk.summary() is not None:
-        line["clocks"] = clk.summary()
+    clocks = clk.summary()
+    if clocks is not None:
+        line["clocks"] = clocks
 
     # end to end through the reference-facing host-pointer call (rec_A_tab_gpu per vector, as
     # jclsquant's kpm_dos_gpu issues it): operator and vector uploads inside the timed region.
@@ -394,7 +465,7 @@ def run_ours(a):
         idx_p = torch.from_numpy(prob["indices"]).pin_memory().numpy()
         vs_p = torch.from_numpy(vs_host).pin_memory().numpy()
         out = torch.zeros((R, M), dtype=torch.complex128).pin_memory().numpy()
-        obv_gpu.rec_A_tab_gpu(data_p, idx_p, L, np.ascontiguousarray(vs_p[0]), out[0], M)  # warm-up
+        obv_gpu.rec_A_tab_gpu(data_p, idx_p, L, np.ascontiguousarray(vs_p[0]), out[0], 16)  # warm-up
         torch.cuda.synchronize()
         barrier(world)
         t0 = time.perf_counter()
@@ -409,6 +480,10 @@ def run_ours(a):
                        "h2d_bytes_per_step": int(R * (prob["data_kpm"].nbytes + prob["indices"].nbytes + n * 16)),
                        "d2h_bytes_per_step": int(R * M * 16),
                        "path": "obv_gpu.rec_A_tab_gpu -> exported rec_A_tab (host pointers, one vector per call)"}
+    if not a.no_batched:
+        del op, v
+        torch.cuda.empty_cache()
+        line["batched_c64"] = run_batched(a, hbm_peak, a.steps, a.warmup)
     if rank == 0 and world == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(prob, a.cpu_seconds)
     if rank == 0:

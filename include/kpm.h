@@ -78,8 +78,17 @@ int kpm_ell_destroy(kpm_ell* h);
 /* Query: n_rows, len_row, 1 if values are stored real, device bytes held. */
 int kpm_ell_info(const kpm_ell* h, int64_t* n_rows, int* len_row, int* is_real,
                  int64_t* device_bytes);
-/* Pre-size the workspace for (dtype, R) so later calls allocate nothing. */
+/* Pre-size the workspace for (dtype, R) so later calls allocate nothing, and
+ * pick the recursion-step kernel for it (the first moment call would otherwise
+ * do this, synchronously). */
 int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M);
+/* Synchronise `stream` and return the status a kernel of h recorded on the
+ * device (KPM_ERR_TIMEOUT if a bounded wait ran out), then clear it. */
+int kpm_ell_check(kpm_ell* h, void* stream);
+/* The recursion-step kernel chosen for (dtype, R): kind 0 = grid-stride,
+ * 1 = bulk-copy staged; rows per thread per tile; CTAs; measured us per step. */
+int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
+                        float* step_us);
 
 /*
  * y <- b*y + a*H x on R vectors ([R][n] c128, device).
@@ -132,6 +141,49 @@ int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int 
 int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u,
                    int M2, const double* c_fd, int M, int len_t, const double* v,
                    double* sigma, void* stream);
+
+/* ---- values update and reverse mode --------------------------------------
+ * No counterpart in the reference (it has no derivatives); they differentiate
+ * rec_A_tab (jclsquant/recurrence_functions.py:9-40).
+ * kpm_ell_set_values: replace the operator values (same reference AoS layout
+ *   and sparsity as at creation; host or device pointer per flags).  A value
+ *   with an imaginary part on a real-stored operator is reported by
+ *   kpm_ell_check as KPM_ERR_DTYPE.
+ * kpm_adjoint_forward: complex128 moments mu[r][m] = <v_r|T_m(H) v_r> (as
+ *   kpm_cheb_moments) of a real symmetric H, keeping (t_k, t_{k+1}) every
+ *   `ckpt` orders for the backward pass.  R in {1, 2, 4, 8}.
+ * kpm_adjoint_backward: for L = sum_r sum_m c[m] Re mu[r][m] (c: device [M]
+ *   doubles) writes grad[i*len_row + s] = dL/dH(i, col(i, s)) (device doubles,
+ *   reference AoS layout), H the rescaled operator; recomputes each checkpoint
+ *   segment and runs the adjoint recursion through it. */
+int kpm_ell_set_values(kpm_ell* h, const double* data, unsigned flags, void* stream);
+int kpm_adjoint_forward(kpm_ell* h, int R, int M, int ckpt, const double* v, double* mu, void* stream);
+int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream);
+
+/* ---- batched operators ---------------------------------------------------
+ * n_inst independent operators of one ELL width, stacked block-diagonally and
+ * advanced by one recursion (one launch per step over all instances, the
+ * whole recursion replayed as one CUDA graph).  The reference runs one
+ * rec_A_tab per instance and vector (jclsquant/recurrence_functions.py:9-40);
+ * this batches that loop.
+ * kpm_batch_create: data/indices are the instances' reference-layout AoS ELL
+ *   arrays concatenated (instance k's rows after instance k-1's), columns local
+ *   to each instance; inst_rows[k] rows each; host pointers.  Values as given
+ *   (pass each instance already rescaled).
+ * kpm_batch_moments: v is device [R][sum_k inst_rows[k]] c128 (instance k at
+ *   its row offset in every vector); mu is device [n_inst][R][M] c128 with
+ *   mu[k][r][m] = <v_r^(k) | T_m(H_k) v_r^(k)>.  R in {1, 2, 4, 8}.
+ *   The first call per (dtype, R, M) records the graph (synchronously).
+ */
+typedef struct kpm_batch_s kpm_batch;
+int kpm_batch_create(kpm_batch** out, int n_inst, const int64_t* inst_rows, int len_row,
+                     const double* data, const int32_t* indices, void* stream);
+int kpm_batch_destroy(kpm_batch* b);
+int kpm_batch_info(const kpm_batch* b, int* n_inst, int64_t* rows_total, int64_t* rows_padded,
+                   int* is_real);
+int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, double* mu,
+                      void* stream);
+int kpm_batch_check(kpm_batch* b, void* stream);
 
 /* ---- reference-compatible host-pointer entry points ---------------------
  * Same names and argument lists as jclsquant/cuda_cython/cuda/obv.h:21-23,30,

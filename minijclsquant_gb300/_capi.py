@@ -43,6 +43,9 @@ SIGNATURES = {
     "kpm_ell_destroy": (_I, [_P]),
     "kpm_ell_info": (_I, [_P, ctypes.POINTER(_I64), ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I64)]),
     "kpm_ell_reserve": (_I, [_P, _I, _I, _I]),
+    "kpm_ell_check": (_I, [_P, _P]),
+    "kpm_ell_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                 ctypes.POINTER(ctypes.c_float)]),
     "kpm_ell_dot": (_I, [_P, _D, _D, _D, _D, _P, _P, _I, _P]),
     "kpm_cheb_moments": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
     "kpm_cheb_series": (_I, [_P, _I, _I, _I, _P, _P, _P, _P]),
@@ -52,6 +55,14 @@ SIGNATURES = {
     "rec_A_tab_2": (None, [_P, _P, _I, _I, _P, _P, _P, _I]),
     "for_time_sigma": (None, [_P, _P, _P, _P, _I, _I, _P, _P, _I, _P, _P, _I, _I]),
     "kpm_last_status": (_I, []),
+    "kpm_ell_set_values": (_I, [_P, _P, _U, _P]),
+    "kpm_adjoint_forward": (_I, [_P, _I, _I, _I, _P, _P, _P]),
+    "kpm_adjoint_backward": (_I, [_P, _P, _P, _P]),
+    "kpm_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _P, _P, _P]),
+    "kpm_batch_destroy": (_I, [_P]),
+    "kpm_batch_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
+    "kpm_batch_moments": (_I, [_P, _I, _I, _I, _P, _P, _P]),
+    "kpm_batch_check": (_I, [_P, _P]),
     "kpm_ell_profile": (_I, [_P, _I]),
     "kpm_ell_profile_read": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "kpm_measure_fp64_fma_rate": (_I, [ctypes.POINTER(_D), _P]),

@@ -1,0 +1,433 @@
+// kpm_batch.cu -- many independent operators of uneven size advanced by one
+// recursion: the instances are stacked block-diagonally into one operator whose
+// rows are padded per instance to a multiple of kRowAlign, so a row tile never
+// spans two instances.  Every step is one launch over all instances (load
+// balance is by tile, not by instance); moment partials are kept per tile and
+// summed per instance by a segmented, fixed-order reduction.  The whole
+// recursion (first step, M-2 steps, reductions) is captured once into a CUDA
+// graph per (precision, R, M) and replayed as a single graph launch.
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "kpm_internal.cuh"
+
+using namespace kpm;
+
+struct kpm_batch_s {
+  int n_inst = 0;
+  int64_t n_total = 0;                 // unpadded rows of all instances
+  std::vector<int64_t> rows;           // per instance
+  std::vector<int64_t> off;            // unpadded row offset (user layout)
+  std::vector<int64_t> poff;           // padded row offset (device layout)
+  int64_t* d_off = nullptr;            // device copies
+  int64_t* d_poff = nullptr;
+  int64_t* d_rows = nullptr;
+  kpm_ell_s* op = nullptr;             // the stacked operator
+  // graph cache
+  struct G {
+    int f32, R, M, kind;
+    const void* bufs[5];  // workspace pointers the graph was recorded with
+    cudaGraphExec_t exec;
+  };
+  std::vector<G> graphs;
+  DevBuf mu_int;                       // internal moments [n_inst][R][M]
+};
+
+namespace {
+
+// padded row -> (instance, local row) by binary search on padded offsets
+__device__ __forceinline__ int find_inst(const int64_t* poff, int n_inst, int64_t prow) {
+  int lo = 0, hi = n_inst - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (poff[mid] <= prow)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void batch_validate_kernel(const double2* __restrict__ data, const int32_t* __restrict__ idx,
+                                      const int64_t* __restrict__ off, const int64_t* __restrict__ rows, int n_inst,
+                                      int L, int64_t n_total, unsigned* flags) {
+  unsigned f = 0;
+  const int64_t count = n_total * L;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t / L;
+    const int k = find_inst(off, n_inst, row);
+    const int32_t c = idx[t];
+    if (c < 0 || (int64_t)c >= rows[k]) f |= 1u;
+    if (data[t].y != 0.0) f |= 2u;
+    if (!isfinite(data[t].x) || !isfinite(data[t].y)) f |= 4u;
+  }
+  if (f) atomicOr(flags, f);
+}
+
+// user AoS (unpadded, local columns) -> padded SoA with global columns, values doubled
+__global__ void batch_repack_kernel(const double2* __restrict__ data, const int32_t* __restrict__ idx,
+                                    const int64_t* __restrict__ off, const int64_t* __restrict__ poff,
+                                    const int64_t* __restrict__ rows, int n_inst, int L, int64_t n_pad, bool real,
+                                    void* val, int32_t* col) {
+  const int64_t total = (int64_t)L * n_pad;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / n_pad);
+    const int64_t prow = t % n_pad;
+    const int k = find_inst(poff, n_inst, prow);
+    const int64_t lr = prow - poff[k];
+    double2 v = make_double2(0.0, 0.0);
+    int32_t c = (int32_t)prow;
+    if (lr < rows[k]) {
+      const int64_t src = (off[k] + lr) * L + s;
+      v = data[src];
+      c = (int32_t)(poff[k] + idx[src]);
+    }
+    col[t] = c;
+    if (real)
+      static_cast<double*>(val)[t] = 2.0 * v.x;
+    else
+      static_cast<double2*>(val)[t] = make_double2(2.0 * v.x, 2.0 * v.y);
+  }
+}
+
+// user vectors [R][n_total] c128 -> padded site-major [n_pad][R]
+__global__ void batch_pack_kernel(const double2* __restrict__ src, const int64_t* __restrict__ off,
+                                  const int64_t* __restrict__ poff, const int64_t* __restrict__ rows, int n_inst,
+                                  int64_t n_total, int64_t n_pad, int R, bool to_f32, void* dst) {
+  const int64_t total = n_pad * R;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t prow = t / R;
+    const int r = (int)(t % R);
+    const int k = find_inst(poff, n_inst, prow);
+    const int64_t lr = prow - poff[k];
+    double2 z = make_double2(0.0, 0.0);
+    if (lr < rows[k]) z = src[(int64_t)r * n_total + off[k] + lr];
+    if (to_f32)
+      static_cast<float2*>(dst)[t] = make_float2((float)z.x, (float)z.y);
+    else
+      static_cast<double2*>(dst)[t] = z;
+  }
+}
+
+// part[step][tile][R] -> mu[k][r][m0 + step], tiles of instance k = [poff_k/TILE, (poff_k + npad_k)/TILE)
+__global__ void batch_reduce_kernel(const double2* __restrict__ part, int64_t ntiles, int tile_rows,
+                                    const int64_t* __restrict__ poff, int64_t n_pad, int n_inst, int R,
+                                    double2* __restrict__ mu, int M, int m0) {
+  const int r = blockIdx.x, k = blockIdx.y, step = blockIdx.z;
+  const int64_t t0 = poff[k] / tile_rows;
+  const int64_t t1 = (k + 1 < n_inst ? poff[k + 1] : n_pad) / tile_rows;
+  const double2* base = part + (int64_t)step * ntiles * R;
+  double sr = 0.0, si = 0.0;
+  for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+    const double2 v = base[t * R + r];
+    sr += v.x;
+    si += v.y;
+  }
+  __shared__ double shr[128], shi[128];
+  shr[threadIdx.x] = sr;
+  shi[threadIdx.x] = si;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      shr[threadIdx.x] += shr[threadIdx.x + w];
+      shi[threadIdx.x] += shi[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) mu[((int64_t)k * R + r) * M + m0 + step] = make_double2(shr[0], shi[0]);
+}
+
+int grid1(int64_t total) { return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 65536)); }
+
+int check_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return KPM_OK;
+  set_last_cuda_error(e);
+  (void)cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? KPM_ERR_OOM : KPM_ERR_CUDA;
+}
+
+// Steps whose per-tile partials are buffered before a segmented reduction.
+int batch_chunk(int64_t ntiles, int R) {
+  const int64_t per_step = ntiles * R * (int64_t)sizeof(double2);
+  int64_t c = ((int64_t)256 << 20) / std::max<int64_t>(1, per_step);
+  return (int)std::max<int64_t>(2, std::min<int64_t>(c, kChunk));
+}
+
+// The launch sequence of one batched recursion on internal buffers:
+// ta = T_0 (packed), tb = T_1, vl = left vectors, part = per-tile partials,
+// mu_int = [n_inst][R][M].
+int record_batched(kpm_batch_s* b, bool f32, int R, int M, const StepConfig& cfg, cudaStream_t s) {
+  kpm_ell_s* h = b->op;
+  Workspace& ws = h->ws;
+  const int tile = cfg.kind == 1 ? staged_tile_rows(f32, R, 1) : kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
+  const int64_t ntiles = h->n_pad / tile;
+  const int chunk = batch_chunk(ntiles, R);
+  double2* part = static_cast<double2*>(ws.part.p);
+  double2* mu = static_cast<double2*>(b->mu_int.p);
+  StepParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.val = f32 ? h->val32 : h->val64;
+  p.col = h->col;
+  p.ld = h->n_pad;
+  p.L = h->L;
+  p.n_pad = h->n_pad;
+  p.a_half = make_double2(0.5, 0.0);
+  p.err = h->err_flag;
+  p.vl = ws.vl.p;
+  p.part_step_stride = ntiles * R;
+  // m = 1 (and mu_0): grid = one CTA per tile of the grid-stride kernel, so its per-CTA
+  // partials are per-tile partials
+  const int tile_simple = kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
+  const int64_t ntiles_simple = h->n_pad / tile_simple;
+  if (ntiles_simple != ntiles) return KPM_ERR_UNSUPPORTED;
+  p.tcur = ws.ta.p;
+  p.tout = ws.tb.p;
+  p.part = part;
+  KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)ntiles, s)
+              : launch_step_f64(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)ntiles, s));
+  void* tprev = ws.ta.p;
+  void* tcur = ws.tb.p;
+  int m0 = 0;
+  for (int m = 2; m < M; ++m) {
+    if (m - m0 == chunk) {
+      dim3 g(R, b->n_inst, chunk);
+      batch_reduce_kernel<<<g, 128, 0, s>>>(part, ntiles, tile, b->d_poff, h->n_pad, b->n_inst, R, mu, M, m0);
+      KPM_CUDA_TRY(cudaGetLastError());
+      m0 = m;
+    }
+    p.tcur = tcur;
+    p.tout = tprev;
+    p.part = part + (int64_t)(m - m0) * ntiles * R;
+    if (cfg.kind == 1) {
+      p.per_tile = 1;
+      KPM_TRY(f32 ? launch_staged_f32(h->is_real, R, 1, p, cfg.grid, s)
+                  : launch_staged_f64(h->is_real, R, 1, p, cfg.grid, s));
+    } else {
+      p.per_tile = 0;
+      KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, (int)ntiles, s)
+                  : launch_step_f64(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, (int)ntiles, s));
+    }
+    std::swap(tprev, tcur);
+  }
+  dim3 g(R, b->n_inst, M - m0);
+  batch_reduce_kernel<<<g, 128, 0, s>>>(part, ntiles, tile, b->d_poff, h->n_pad, b->n_inst, R, mu, M, m0);
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpm_batch_create(kpm_batch** out, int n_inst, const int64_t* inst_rows, int len_row, const double* data,
+                     const int32_t* indices, void* stream) {
+  if (!out || n_inst < 1 || !inst_rows || len_row < 1 || !data || !indices) return KPM_ERR_INVALID_ARG;
+  *out = nullptr;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  kpm_batch_s* b = new kpm_batch_s();
+  b->n_inst = n_inst;
+  b->rows.assign(inst_rows, inst_rows + n_inst);
+  int64_t o = 0, po = 0;
+  for (int k = 0; k < n_inst; ++k) {
+    if (b->rows[k] < 1) {
+      delete b;
+      return KPM_ERR_INVALID_ARG;
+    }
+    b->off.push_back(o);
+    b->poff.push_back(po);
+    o += b->rows[k];
+    po += ((b->rows[k] + kRowAlign - 1) / kRowAlign) * kRowAlign;
+  }
+  b->n_total = o;
+  if (po > (int64_t)INT32_MAX) {
+    delete b;
+    return KPM_ERR_SHAPE;
+  }
+  kpm_ell_s* h = new kpm_ell_s();
+  b->op = h;
+  h->n = po;  // every padded row is a row of the stacked operator
+  h->n_pad = po;
+  h->L = len_row;
+  int dev = 0;
+  DevBuf st_data, st_idx, flag;
+  auto fail = [&](int code) {
+    release(st_data);
+    release(st_idx);
+    release(flag);
+    kpm_batch_destroy(b);
+    return code;
+  };
+  int rc = check_cuda(cudaGetDevice(&dev));
+  if (rc == KPM_OK) rc = check_cuda(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev));
+  if (rc != KPM_OK) return fail(rc);
+  h->device = dev;
+  const int64_t count = b->n_total * len_row;
+  if ((rc = ensure(st_data, count * sizeof(double2))) != KPM_OK) return fail(rc);
+  if ((rc = ensure(st_idx, count * sizeof(int32_t))) != KPM_OK) return fail(rc);
+  if ((rc = ensure(flag, sizeof(unsigned))) != KPM_OK) return fail(rc);
+  rc = check_cuda(cudaMalloc(reinterpret_cast<void**>(&b->d_off), n_inst * sizeof(int64_t)));
+  if (rc == KPM_OK) rc = check_cuda(cudaMalloc(reinterpret_cast<void**>(&b->d_poff), n_inst * sizeof(int64_t)));
+  if (rc == KPM_OK) rc = check_cuda(cudaMalloc(reinterpret_cast<void**>(&b->d_rows), n_inst * sizeof(int64_t)));
+  if (rc != KPM_OK) return fail(rc);
+  rc = check_cuda(cudaMemcpyAsync(st_data.p, data, count * sizeof(double2), cudaMemcpyHostToDevice, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(st_idx.p, indices, count * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(b->d_off, b->off.data(), n_inst * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(b->d_poff, b->poff.data(), n_inst * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(b->d_rows, b->rows.data(), n_inst * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(flag.p, 0, sizeof(unsigned), s));
+  if (rc != KPM_OK) return fail(rc);
+  batch_validate_kernel<<<grid1(count), 256, 0, s>>>(static_cast<const double2*>(st_data.p),
+                                                      static_cast<const int32_t*>(st_idx.p), b->d_off, b->d_rows,
+                                                      n_inst, len_row, b->n_total, static_cast<unsigned*>(flag.p));
+  unsigned hf = 0;
+  rc = check_cuda(cudaGetLastError());
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(&hf, flag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaStreamSynchronize(s));
+  if (rc != KPM_OK) return fail(rc);
+  if (hf & 1u) return fail(KPM_ERR_INDEX);
+  if (hf & 4u) return fail(KPM_ERR_NONFINITE);
+  h->is_real = (hf & 2u) ? 0 : 1;
+  const int64_t slots = (int64_t)len_row * h->n_pad;
+  rc = check_cuda(cudaMalloc(&h->val64, slots * (h->is_real ? sizeof(double) : sizeof(double2))));
+  if (rc == KPM_OK) rc = check_cuda(cudaMalloc(reinterpret_cast<void**>(&h->col), slots * sizeof(int32_t)));
+  if (rc == KPM_OK) rc = check_cuda(cudaMalloc(reinterpret_cast<void**>(&h->err_flag), sizeof(int)));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(h->err_flag, 0, sizeof(int), s));
+  if (rc != KPM_OK) return fail(rc);
+  batch_repack_kernel<<<grid1(slots), 256, 0, s>>>(static_cast<const double2*>(st_data.p),
+                                                    static_cast<const int32_t*>(st_idx.p), b->d_off, b->d_poff,
+                                                    b->d_rows, n_inst, len_row, h->n_pad, h->is_real != 0, h->val64,
+                                                    h->col);
+  rc = check_cuda(cudaGetLastError());
+  if (rc == KPM_OK) rc = check_cuda(cudaStreamSynchronize(s));
+  if (rc != KPM_OK) return fail(rc);
+  release(st_data);
+  release(st_idx);
+  release(flag);
+  *out = b;
+  return KPM_OK;
+}
+
+int kpm_batch_destroy(kpm_batch* b) {
+  if (!b) return KPM_ERR_INVALID_ARG;
+  for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  release(b->mu_int);
+  if (b->d_off) cudaFree(b->d_off);
+  if (b->d_poff) cudaFree(b->d_poff);
+  if (b->d_rows) cudaFree(b->d_rows);
+  if (b->op) kpm_ell_destroy(b->op);
+  delete b;
+  return KPM_OK;
+}
+
+int kpm_batch_info(const kpm_batch* b, int* n_inst, int64_t* rows_total, int64_t* rows_padded, int* is_real) {
+  if (!b) return KPM_ERR_INVALID_ARG;
+  if (n_inst) *n_inst = b->n_inst;
+  if (rows_total) *rows_total = b->n_total;
+  if (rows_padded) *rows_padded = b->op->n_pad;
+  if (is_real) *is_real = b->op->is_real;
+  return KPM_OK;
+}
+
+int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, double* mu, void* stream) {
+  if (!b || !v || !mu || M < 2) return KPM_ERR_INVALID_ARG;
+  if (dtype != KPM_C128 && dtype != KPM_C64) return KPM_ERR_DTYPE;
+  if (R != 1 && R != 2 && R != 4 && R != 8) return KPM_ERR_UNSUPPORTED;
+  const bool f32 = dtype == KPM_C64;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  kpm_ell_s* h = b->op;
+  if (f32) KPM_TRY(ensure_f32_values(h, s));
+  const size_t vb = (size_t)h->n_pad * R * (f32 ? sizeof(float2) : sizeof(double2));
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  KPM_TRY(ensure(b->mu_int, (size_t)b->n_inst * R * M * sizeof(double2)));
+  // kernel choice: staged (one row per thread, per-tile partials) or grid-stride, timed once
+  StepConfig cfg;
+  {
+    const int key = (f32 ? 1000 : 0) + R * 10 + 9;  // batched entries are keyed apart from plain ones
+    bool found = false;
+    for (auto& kv : h->tuned)
+      if (kv.first == key) {
+        cfg = kv.second;
+        found = true;
+      }
+    if (!found) {
+      const int occ = f32 ? staged_ctas_f32(h->is_real, R, 1, h->L, 2) : staged_ctas_f64(h->is_real, R, 1, h->L, 2);
+      const int tile = staged_tile_rows(f32, R, 1);
+      const int64_t ntiles = h->n_pad / tile;
+      cfg.kind = occ > 0 ? 1 : 0;
+      cfg.U = 1;
+      cfg.grid = occ > 0 ? (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count)) : (int)ntiles;
+      const char* force = getenv("KPM_STEP_KERNEL");
+      if (force && std::string(force) == "simple") {
+        cfg.kind = 0;
+        cfg.grid = (int)ntiles;
+      }
+      h->tuned.emplace_back(key, cfg);
+    }
+  }
+  const int tile = staged_tile_rows(f32, R, 1);
+  const int64_t ntiles = h->n_pad / tile;
+  KPM_TRY(ensure(ws.part, (size_t)batch_chunk(ntiles, R) * ntiles * R * sizeof(double2)));
+  // inputs into the internal buffers (outside the graph)
+  batch_pack_kernel<<<grid1(h->n_pad * R), 256, 0, s>>>(reinterpret_cast<const double2*>(v), b->d_off, b->d_poff,
+                                                         b->d_rows, b->n_inst, b->n_total, h->n_pad, R, f32, ws.ta.p);
+  KPM_CUDA_TRY(cudaGetLastError());
+  KPM_CUDA_TRY(cudaMemcpyAsync(ws.vl.p, ws.ta.p, vb, cudaMemcpyDeviceToDevice, s));
+  // the recursion: one graph launch (re-recorded if a workspace buffer moved)
+  const void* bufs[5] = {ws.ta.p, ws.tb.p, ws.vl.p, ws.part.p, b->mu_int.p};
+  cudaGraphExec_t exec = nullptr;
+  for (size_t i = 0; i < b->graphs.size(); ++i) {
+    auto& g = b->graphs[i];
+    if (g.f32 == (int)f32 && g.R == R && g.M == M && g.kind == cfg.kind) {
+      if (std::equal(bufs, bufs + 5, g.bufs)) {
+        exec = g.exec;
+      } else {
+        cudaGraphExecDestroy(g.exec);
+        b->graphs.erase(b->graphs.begin() + i);
+      }
+      break;
+    }
+  }
+  const bool use_graph = getenv("KPM_NO_GRAPH") == nullptr;
+  if (!use_graph) {
+    KPM_TRY(record_batched(b, f32, R, M, cfg, s));
+  } else {
+    if (!exec) {
+      cudaStream_t cs;
+      KPM_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      cudaGraph_t graph;
+      KPM_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+      const int rc = record_batched(b, f32, R, M, cfg, cs);
+      const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+      cudaStreamDestroy(cs);
+      if (rc != KPM_OK) return rc;
+      KPM_CUDA_TRY(ec);
+      const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      KPM_CUDA_TRY(ei);
+      kpm_batch_s::G g;
+      g.f32 = (int)f32;
+      g.R = R;
+      g.M = M;
+      g.kind = cfg.kind;
+      std::copy(bufs, bufs + 5, g.bufs);
+      g.exec = exec;
+      b->graphs.push_back(g);
+    }
+    KPM_CUDA_TRY(cudaGraphLaunch(exec, s));
+  }
+  KPM_CUDA_TRY(cudaMemcpyAsync(mu, b->mu_int.p, (size_t)b->n_inst * R * M * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  return KPM_OK;
+}
+
+int kpm_batch_check(kpm_batch* b, void* stream) {
+  if (!b) return KPM_ERR_INVALID_ARG;
+  return kpm_ell_check(b->op, stream);
+}
+
+}  // extern "C"

@@ -3,7 +3,9 @@
 // reference-compatible host-pointer entry points.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "kpm_internal.cuh"
@@ -61,6 +63,11 @@ int grid_1d(int64_t total) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(g, 65536));
 }
 
+}  // namespace
+
+// Driver helpers shared with the other translation units (declared in kpm_internal.cuh).
+namespace kpm {
+
 int pow2_group(int remaining) {
   if (remaining >= 8) return 8;
   if (remaining >= 4) return 4;
@@ -80,6 +87,7 @@ StepParams base_params(kpm_ell_s* h, bool f32) {
   p.n_pad = h->n_pad;
   p.a_half = make_double2(0.5, 0.0);
   p.b = make_double2(0.0, 0.0);
+  p.err = h->err_flag;
   return p;
 }
 
@@ -87,13 +95,105 @@ int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams&
   return f32 ? launch_step_f32(real, R, mode, epi, p, grid, s) : launch_step_f64(real, R, mode, epi, p, grid, s);
 }
 
+int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s) {
+  if (cfg.kind == 1)
+    return f32 ? launch_staged_f32(real, R, cfg.U, p, cfg.grid, s) : launch_staged_f64(real, R, cfg.U, p, cfg.grid, s);
+  return launch_step(f32, real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, cfg.grid, s);
+}
+
+// Choose the MODE_NEXT kernel for (precision, R group, moment sets): the
+// grid-stride kernel or the staged kernel with 1 or 2 rows per thread, each
+// with a full wave of resident CTAs.  When several fit, each is timed on the
+// operator itself (a few launches on zeroed workspace vectors) and the fastest
+// is kept for the handle's lifetime.  KPM_STEP_KERNEL=simple|staged1|staged2
+// forces one.
+int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out) {
+  const int key = (f32 ? 1000 : 0) + Rg * 10 + sets;
+  for (auto& kv : h->tuned)
+    if (kv.first == key) {
+      *out = kv.second;
+      return KPM_OK;
+    }
+  std::vector<StepConfig> cands;
+  const char* force = getenv("KPM_STEP_KERNEL");
+  const std::string f = force ? force : "";
+  if (f.empty() || f == "simple") {
+    StepConfig c;
+    c.kind = 0;
+    c.grid = grid_for(h, Rg, vpt_for(f32, Rg));
+    cands.push_back(c);
+  }
+  // the staged kernel serves one moment set; two-set calls use the grid-stride kernel
+  for (int U = 1; U <= 2 && sets == 1; ++U) {
+    if (!f.empty() && f != (U == 1 ? "staged1" : "staged2")) continue;
+    const int occ = f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2) : staged_ctas_f64(h->is_real, Rg, U, h->L, 2);
+    if (occ <= 0) continue;
+    const int64_t ntiles = h->n_pad / staged_tile_rows(f32, Rg, U);
+    StepConfig c;
+    c.kind = 1;
+    c.U = U;
+    c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
+    cands.push_back(c);
+  }
+  if (cands.empty()) {  // a forced staged kernel that cannot serve this call (two moment sets)
+    StepConfig c;
+    c.kind = 0;
+    c.grid = grid_for(h, Rg, vpt_for(f32, Rg));
+    cands.push_back(c);
+  }
+  if (cands.size() > 1) {
+    int max_grid = 0;
+    for (auto& c : cands) max_grid = std::max(max_grid, c.grid);
+    const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+    Workspace& ws = h->ws;
+    KPM_TRY(ensure(ws.ta, vb));
+    KPM_TRY(ensure(ws.tb, vb));
+    KPM_TRY(ensure(ws.vl, vb));
+    if (sets == 2) KPM_TRY(ensure(ws.vr, vb));
+    KPM_TRY(ensure(ws.part, (size_t)kChunk * sets * max_grid * Rg * sizeof(double2)));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.ta.p, 0, vb, s));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.tb.p, 0, vb, s));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.vl.p, 0, vb, s));
+    if (sets == 2) KPM_CUDA_TRY(cudaMemsetAsync(ws.vr.p, 0, vb, s));
+    StepParams p = base_params(h, f32);
+    p.tcur = ws.ta.p;
+    p.tout = ws.tb.p;
+    p.vl = ws.vl.p;
+    p.vl2 = sets == 2 ? ws.vr.p : nullptr;
+    p.part = static_cast<double2*>(ws.part.p);
+    cudaEvent_t e0, e1;
+    KPM_CUDA_TRY(cudaEventCreate(&e0));
+    KPM_CUDA_TRY(cudaEventCreate(&e1));
+    const int reps = 3;
+    for (auto& c : cands) {
+      KPM_TRY(launch_next(f32, h->is_real, Rg, c, p, s));
+      KPM_CUDA_TRY(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps; ++r) KPM_TRY(launch_next(f32, h->is_real, Rg, c, p, s));
+      KPM_CUDA_TRY(cudaEventRecord(e1, s));
+      KPM_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      KPM_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+      c.us = 1e3f * ms / reps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  StepConfig best = cands[0];
+  for (auto& c : cands)
+    if (c.us < best.us) best = c;
+  h->tuned.emplace_back(key, best);
+  *out = best;
+  return KPM_OK;
+}
+
 // Moments for one group of Rg <= 8 vectors starting at r0.
 int moments_group(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const double* v_r, const double* v_l,
                   double* mu, double* mu_rr, cudaStream_t s) {
-  const int vpt = vpt_for(f32, Rg);
-  const int grid = grid_for(h, Rg, vpt);
   const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
   const int sets = mu_rr ? 2 : 1;
+  StepConfig cfg;
+  KPM_TRY(step_config(h, f32, Rg, sets, s, &cfg));
+  const int grid = cfg.grid;
   Workspace& ws = h->ws;
   KPM_TRY(ensure(ws.ta, vb));
   KPM_TRY(ensure(ws.tb, vb));
@@ -129,7 +229,7 @@ int moments_group(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const do
     p.tcur = tcur;
     p.tout = tprev;
     p.part = part + (int64_t)(m - m0) * step_stride;
-    KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_NEXT, EPI_STORE | EPI_MOM1, p, grid, s));
+    KPM_TRY(launch_next(f32, h->is_real, Rg, cfg, p, s));
     std::swap(tprev, tcur);
   }
   if (M > 2) KPM_TRY(prof_end(h, s, ev, M - 2));
@@ -167,7 +267,7 @@ int series_packed(kpm_ell_s* h, bool f32, int Rg, int M, const double2* coef, co
 
 int check_dtype(int dtype) { return (dtype == KPM_C128 || dtype == KPM_C64) ? KPM_OK : KPM_ERR_DTYPE; }
 
-}  // namespace
+}  // namespace kpm
 
 extern "C" {
 
@@ -255,6 +355,8 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
   const int64_t slots = (int64_t)len_row * h->n_pad;
   e = cudaMalloc(&h->val64, slots * (h->is_real ? sizeof(double) : sizeof(double2)));
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->col), slots * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->err_flag), sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->err_flag, 0, sizeof(int), s);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
     (void)cudaGetLastError();
@@ -280,8 +382,10 @@ int kpm_ell_destroy(kpm_ell* h) {
   if (h->val64) cudaFree(h->val64);
   if (h->val32) cudaFree(h->val32);
   if (h->col) cudaFree(h->col);
+  if (h->err_flag) cudaFree(h->err_flag);
   Workspace& w = h->ws;
-  DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef};
+  DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef,
+                    &w.ckpt, &w.seg, &w.grad};
   for (DevBuf* b : bufs) release(*b);
   kpm_ell_profile(h, 0);
   delete h;
@@ -298,7 +402,8 @@ int kpm_ell_info(const kpm_ell* h, int64_t* n_rows, int* len_row, int* is_real, 
     int64_t b = slots * (h->is_real ? 8 : 16) + slots * 4;
     if (h->val32) b += slots * (h->is_real ? 4 : 8);
     const Workspace& w = h->ws;
-    const DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef};
+    const DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef,
+                            &w.ckpt, &w.seg, &w.grad};
     for (const DevBuf* d : bufs) b += (int64_t)d->bytes;
     *device_bytes = b;
   }
@@ -317,7 +422,10 @@ int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M) {
   KPM_TRY(ensure(ws.tb, vb));
   KPM_TRY(ensure(ws.vl, vb));
   KPM_TRY(ensure(ws.vr, vb));
-  const int grid = grid_for(h, Rg, vpt_for(f32, Rg));
+  StepConfig c1, c2;
+  KPM_TRY(step_config(h, f32, Rg, 1, nullptr, &c1));
+  KPM_TRY(step_config(h, f32, Rg, 2, nullptr, &c2));
+  const int grid = std::max(c1.grid, c2.grid);
   KPM_TRY(ensure(ws.part, (size_t)kChunk * 2 * grid * Rg * sizeof(double2)));
   KPM_CUDA_TRY(cudaDeviceSynchronize());
   return KPM_OK;
@@ -446,6 +554,33 @@ int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const
 }
 
 int kpm_last_status(void) { return g_last_status; }
+
+int kpm_ell_check(kpm_ell* h, void* stream) {
+  if (!h) return KPM_ERR_INVALID_ARG;
+  cudaStream_t s = as_stream(stream);
+  int flag = 0;
+  KPM_CUDA_TRY(cudaMemcpyAsync(&flag, h->err_flag, sizeof(int), cudaMemcpyDeviceToHost, s));
+  KPM_CUDA_TRY(cudaStreamSynchronize(s));
+  if (flag != 0) {
+    KPM_CUDA_TRY(cudaMemsetAsync(h->err_flag, 0, sizeof(int), s));
+    return flag;
+  }
+  return KPM_OK;
+}
+
+int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid, float* step_us) {
+  if (!h || R < 1) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  const int Rg = pow2_group(R);
+  if (dtype == KPM_C64) KPM_TRY(ensure_f32_values(h, nullptr));
+  StepConfig cfg;
+  KPM_TRY(step_config(h, dtype == KPM_C64, Rg, 1, nullptr, &cfg));
+  if (kind) *kind = cfg.kind;
+  if (rows_per_thread) *rows_per_thread = cfg.U;
+  if (grid) *grid = cfg.grid;
+  if (step_us) *step_us = cfg.us;
+  return KPM_OK;
+}
 
 // ---- reference-compatible host-pointer entry points -------------------------
 static int host_rec(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l, double* v_r,

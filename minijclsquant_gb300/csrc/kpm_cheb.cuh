@@ -83,6 +83,44 @@ __device__ __forceinline__ void madd(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x)
   }
 }
 
+// acc = h * x - old: the first slot of a recursion row, with -T_{m-1} folded
+// into the addend of the multiply-add (no separate negation).
+template <typename T, int VPT>
+__device__ __forceinline__ void madd_first_neg(Cx<T, VPT>& acc, T h, const Cx<T, VPT>& x, const Cx<T, VPT>& old) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = fma(h, x.re[k], -old.re[k]);
+    acc.im[k] = fma(h, x.im[k], -old.im[k]);
+  }
+}
+template <typename T, int VPT, typename C2>
+__device__ __forceinline__ void madd_first_neg(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x, const Cx<T, VPT>& old) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = fma(h.x, x.re[k], -old.re[k]);
+    acc.re[k] = fma(-h.y, x.im[k], acc.re[k]);
+    acc.im[k] = fma(h.x, x.im[k], -old.im[k]);
+    acc.im[k] = fma(h.y, x.re[k], acc.im[k]);
+  }
+}
+// acc = h * x (first slot without a previous vector).
+template <typename T, int VPT>
+__device__ __forceinline__ void mul_first(Cx<T, VPT>& acc, T h, const Cx<T, VPT>& x) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = h * x.re[k];
+    acc.im[k] = h * x.im[k];
+  }
+}
+template <typename T, int VPT, typename C2>
+__device__ __forceinline__ void mul_first(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = fma(-h.y, x.im[k], h.x * x.re[k]);
+    acc.im[k] = fma(h.y, x.re[k], h.x * x.im[k]);
+  }
+}
+
 // conj(l) * t, accumulated into (re, im).
 template <typename A, typename T>
 __device__ __forceinline__ void cdot_acc(A& re, A& im, T lr, T li, T tr, T ti) {
@@ -178,38 +216,40 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
     const int64_t vi = row * TPR + sub;
     Cx<T, VPT> acc;
     Cx<T, VPT> old;
-    if (MODE == MODE_NEXT || (MODE == MODE_APPLY && p.b.x != 0.0) || (MODE == MODE_APPLY && p.b.y != 0.0)) {
+    if (MODE == MODE_NEXT && p.tprev != nullptr) {
+      unpack(static_cast<const Raw*>(p.tprev)[vi], old);
+    } else if (MODE == MODE_NEXT || (MODE == MODE_APPLY && p.b.x != 0.0) || (MODE == MODE_APPLY && p.b.y != 0.0)) {
       unpack(tout[vi], old);
     } else {
 #pragma unroll
       for (int k = 0; k < VPT; ++k) old.re[k] = old.im[k] = T(0);
     }
-#pragma unroll
-    for (int k = 0; k < VPT; ++k) {
-      acc.re[k] = (MODE == MODE_NEXT) ? -old.re[k] : T(0);
-      acc.im[k] = (MODE == MODE_NEXT) ? -old.im[k] : T(0);
-    }
-    int s = 0;
-    for (; s + 4 <= L; s += 4) {
+    // slots in groups of four: all loads of a group are issued before its FMAs;
+    // the first slot folds -T_{m-1} into its multiply-add.
+    for (int s = 0; s < L; s += 4) {
       int c[4];
       MV h[4];
       Cx<T, VPT> x[4];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        c[u] = __ldcs(col + (int64_t)(s + u) * ld + row);
-        h[u] = __ldcs(val + (int64_t)(s + u) * ld + row);
+      for (int u = 0; u < 4; ++u)
+        if (s + u < L) {
+          c[u] = __ldcs(col + (int64_t)(s + u) * ld + row);
+          h[u] = __ldcs(val + (int64_t)(s + u) * ld + row);
+        }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (s + u < L) unpack(__ldg(tcur + (int64_t)c[u] * TPR + sub), x[u]);
+      if (s == 0) {
+        if (MODE == MODE_NEXT)
+          madd_first_neg(acc, h[0], x[0], old);
+        else
+          mul_first(acc, h[0], x[0]);
+      } else {
+        madd(acc, h[0], x[0]);
       }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) unpack(__ldg(tcur + (int64_t)c[u] * TPR + sub), x[u]);
-#pragma unroll
-      for (int u = 0; u < 4; ++u) madd(acc, h[u], x[u]);
-    }
-    for (; s < L; ++s) {
-      const int c = __ldcs(col + (int64_t)s * ld + row);
-      const MV h = __ldcs(val + (int64_t)s * ld + row);
-      Cx<T, VPT> x;
-      unpack(__ldg(tcur + (int64_t)c * TPR + sub), x);
-      madd(acc, h, x);
+      for (int u = 1; u < 4; ++u)
+        if (s + u < L) madd(acc, h[u], x[u]);
     }
     if (MODE == MODE_FIRST) {
 #pragma unroll

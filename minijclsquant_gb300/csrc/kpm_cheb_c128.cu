@@ -1,5 +1,5 @@
-// Complex128 instantiations of the fused step kernel (the drop-in form).
-#include "kpm_cheb.cuh"
+// Complex128 instantiations of the step kernels (the drop-in form).
+#include "kpm_staged.cuh"
 
 namespace kpm {
 
@@ -20,6 +20,14 @@ int launch_step_f64(bool real, int R, int mode, int epi, const StepParams& p, in
     default:
       return KPM_ERR_UNSUPPORTED;
   }
+}
+
+int launch_staged_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+  return Staged<double>::launch(real, R, U, p, grid, s);
+}
+
+int staged_ctas_f64(bool real, int R, int U, int L, int nvec) {
+  return Staged<double>::ctas_per_sm(real, R, U, L, nvec);
 }
 
 }  // namespace kpm

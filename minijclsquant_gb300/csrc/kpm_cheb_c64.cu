@@ -1,7 +1,7 @@
-// Complex64 instantiations of the fused step kernel (mixed precision: complex64
+// Complex64 instantiations of the step kernels (mixed precision: complex64
 // vectors and values, FP64 moment accumulation).  Two complex64 values per
 // thread make every access a 16-byte vector load.
-#include "kpm_cheb.cuh"
+#include "kpm_staged.cuh"
 
 namespace kpm {
 
@@ -22,6 +22,14 @@ int launch_step_f32(bool real, int R, int mode, int epi, const StepParams& p, in
     default:
       return KPM_ERR_UNSUPPORTED;
   }
+}
+
+int launch_staged_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+  return Staged<float>::launch(real, R, U, p, grid, s);
+}
+
+int staged_ctas_f32(bool real, int R, int U, int L, int nvec) {
+  return Staged<float>::ctas_per_sm(real, R, U, L, nvec);
 }
 
 }  // namespace kpm

@@ -26,7 +26,7 @@
 namespace kpm {
 
 constexpr int kBlock = 256;       // threads per CTA of every streaming kernel
-constexpr int kRowAlign = 256;    // n_pad is a multiple of this
+constexpr int kRowAlign = 512;    // n_pad is a multiple of this (and of every staged tile)
 constexpr int kMaxGroupR = 8;     // vectors advanced together by one launch
 constexpr int kChunk = 128;       // recursion steps whose moment partials are buffered
 
@@ -61,6 +61,15 @@ struct Workspace {
   DevBuf acc, acc2;        // series accumulators
   DevBuf part;             // per-CTA moment partials [kChunk][sets][grid][R] double2
   DevBuf coef;             // small device staging (coefficients)
+  DevBuf ckpt, seg, grad;  // adjoint: checkpoint pairs, recomputed segment, per-slot gradient
+};
+
+// Kernel choice for the recursion step of one (precision, R group, moment sets).
+struct StepConfig {
+  int kind = 0;  // 0: grid-stride kernel, 1: bulk-copy staged kernel
+  int U = 1;     // rows per thread per tile (staged)
+  int grid = 0;  // CTAs
+  float us = 0;  // measured time of one step launch when tuned
 };
 
 }  // namespace kpm
@@ -80,6 +89,12 @@ struct kpm_ell_s {
   int prof = 0;
   int64_t prof_launches = 0;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof_events;
+  // device status word written by kernels whose bounded waits ran out
+  int* err_flag = nullptr;
+  // tuned step kernels, key = f32 * 1000 + R * 10 + sets
+  std::vector<std::pair<int, kpm::StepConfig>> tuned;
+  // the forward pass the next kpm_adjoint_backward differentiates
+  int adj_R = 0, adj_M = 0, adj_ckpt = 0;
 };
 
 namespace kpm {
@@ -103,6 +118,9 @@ struct StepParams {
   int m;                  // recursion index of the vector being produced
   double2 a_half;         // APPLY: a/2 (values are 2H)
   double2 b;              // APPLY: b
+  int* err;               // device status word (KPM_ERR_TIMEOUT from a bounded wait)
+  int per_tile;           // staged kernel: partials per tile ([sets][tiles][R]) instead of per CTA
+  const void* tprev;      // grid-stride MODE_NEXT: read T_{m-1} here instead of tout (out of place)
 };
 
 // Launch helpers implemented per precision (kpm_cheb_c128.cu, kpm_cheb_c64.cu).
@@ -111,6 +129,25 @@ enum Epi { EPI_STORE = 1, EPI_MOM1 = 2, EPI_MOM2 = 4, EPI_SERIES = 8, EPI_APPLY_
 
 int launch_step_f64(bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
 int launch_step_f32(bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
+// Bulk-copy staged MODE_NEXT step (kpm_staged.cuh), and how many of its CTAs fit one SM.
+int launch_staged_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
+int launch_staged_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
+int staged_ctas_f64(bool real, int R, int U, int L, int nvec);
+int staged_ctas_f32(bool real, int R, int U, int L, int nvec);
+// Driver helpers (kpm_capi.cu).
+int pow2_group(int remaining);
+int vpt_for(bool f32, int Rg);
+StepParams base_params(kpm_ell_s* h, bool f32);
+int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
+int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s);
+int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out);
+int check_dtype(int dtype);
+
+// Rows per tile of the staged kernel (complex64 packs two vectors per thread).
+inline int staged_tile_rows(bool f32, int R, int U) {
+  const int vpt = (f32 && R >= 2) ? 2 : 1;
+  return (kBlock / (R / vpt)) * U;
+}
 int grid_for(const kpm_ell_s* h, int R, int vpt);
 
 // Layout helpers (kpm_util.cu).

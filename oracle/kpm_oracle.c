@@ -243,3 +243,44 @@ int oracle_max_threads(void) {
   return 1;
 #endif
 }
+
+/* Gradient of L = sum_m c_m Re <v|T_m(A) v> with respect to every ELL slot
+ * value of a real symmetric A (no reference counterpart: the reference has no
+ * derivatives).  Stores every t_m = T_m(A) v, then runs the adjoint recursion
+ *   lambda_m = c_m conj(v) + 2 A lambda_{m+1} - lambda_{m+2},  m = M-1 .. 1,
+ * and accumulates grad[i*L + s] = Re[w_m lambda_m[i] t_{m-1}[col(i,s)]] with
+ * w_1 = 1, w_m = 2 otherwise.  The forward recursion is the oracle's own
+ * (rec_A_tab, recurrence_functions.py:9-40); `data` is complex128 with zero
+ * imaginary parts.  Returns 0, or -1 on bad arguments / allocation failure. */
+int oracle_adjoint_grad(int M, const zc* data, const int32_t* indices, int len_row, int n, const zc* v,
+                        const double* c, double* grad) {
+  if (M < 2 || n < 1 || len_row < 1) return -1;
+  zc* t = (zc*)calloc((size_t)M * (size_t)n, sizeof(zc));
+  zc* la = (zc*)calloc((size_t)n, sizeof(zc));
+  zc* lb = (zc*)calloc((size_t)n, sizeof(zc));
+  zc* ln = (zc*)calloc((size_t)n, sizeof(zc));
+  if (!t || !la || !lb || !ln) { free(t); free(la); free(lb); free(ln); return -1; }
+  memcpy(t, v, sizeof(zc) * (size_t)n);
+  if (M > 1) oracle_aAxby(1.0, 0.0, 0.0, 0.0, t, t + n, data, indices, len_row, n, 1);
+  for (int m = 2; m < M; ++m) {
+    zc* out = t + (size_t)m * n;
+    memcpy(out, t + (size_t)(m - 2) * n, sizeof(zc) * (size_t)n);
+    oracle_aAxby(2.0, 0.0, -1.0, 0.0, t + (size_t)(m - 1) * n, out, data, indices, len_row, n, 1);
+  }
+  memset(grad, 0, sizeof(double) * (size_t)n * len_row);
+  /* la = lambda_{m+1}, lb = lambda_{m+2} */
+  for (int m = M - 1; m >= 1; --m) {
+    for (int i = 0; i < n; ++i) ln[i] = c[m] * conj(v[i]) - lb[i];
+    oracle_aAxby(2.0, 0.0, 1.0, 0.0, la, ln, data, indices, len_row, n, 1);
+    const double w = m == 1 ? 1.0 : 2.0;
+    const zc* tp = t + (size_t)(m - 1) * n;
+    for (int i = 0; i < n; ++i)
+      for (int s = 0; s < len_row; ++s) {
+        const int64_t q = (int64_t)i * len_row + s;
+        grad[q] += w * creal(ln[i] * tp[indices[q]]);
+      }
+    zc* tmp = lb; lb = la; la = ln; ln = tmp;
+  }
+  free(t); free(la); free(lb); free(ln);
+  return 0;
+}

@@ -36,6 +36,7 @@ def lib():
         c.oracle_rec_com_A_vec.argtypes = [I, P, P, P, I, I, P, P, P, I]
         c.oracle_for_time_sigma.argtypes = [P, P, P, P, I, I, P, P, I, P, P, I, I, I]
         c.oracle_max_threads.restype = I
+        c.oracle_adjoint_grad.argtypes = [I, P, P, I, I, P, P, P]
         _lib = c
     return _lib
 
@@ -144,3 +145,13 @@ def moment_tolerance_ok(mu, ref, rel=1e-10, floor_frac=1e-6):
     scale = np.maximum(np.abs(ref), floor_frac * np.abs(ref[..., :1]))
     err = np.abs(mu - ref) / scale
     return bool(np.all(err <= rel)), float(np.max(err))
+
+
+def adjoint_grad(M, data, indices, len_row, v, c):
+    """d/dH(slot) of sum_m c_m Re <v|T_m v> for real symmetric H (all t_m stored)."""
+    data, indices, v = _c(data, np.complex128), _c(indices, np.int32), _c(v, np.complex128)
+    c = _c(c, np.float64)
+    grad = np.zeros(data.size, dtype=np.float64)
+    _check(lib().oracle_adjoint_grad(int(M), data.ctypes.data, indices.ctypes.data, int(len_row), v.size,
+                                     v.ctypes.data, c.ctypes.data, grad.ctypes.data), "adjoint_grad")
+    return grad

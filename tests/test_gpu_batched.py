@@ -1,0 +1,98 @@
+"""Batched operators (uneven instances in one recursion) against the oracle,
+one instance at a time.  Complex128 tolerance as the plain path (1e-10 per
+order); complex64 against its own error budget."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-10
+
+
+def _ensemble(n_inst, side_range, seed):
+    from minijclsquant_gb300 import batched
+
+    return batched.honeycomb_ensemble(n_inst, side_range=side_range, W_range=(0.0, 2.0), seed=seed)
+
+
+@pytest.mark.parametrize("R", [1, 2, 4, 8])
+def test_batched_c128_matches_oracle_per_instance(cuda_lib, R):
+    from minijclsquant_gb300 import batched
+
+    datas, idxs, L, bnds, _ = _ensemble(7, (2, 23), seed=3 + R)  # 8 .. 1058 sites, some under one tile
+    B = batched.BatchedELL(datas, idxs, L)
+    v = batched.ensemble_vectors(B.rows, R, seed0=500)
+    M = 140
+    mu = B.moments(M, v, dtype="c128")
+    assert mu.shape == (7, R, M)
+    for k in range(7):
+        o, n = int(B.offsets[k]), int(B.rows[k])
+        for r in range(R):
+            ref = oracle.rec_A_tab(M, datas[k], idxs[k], L, v[r, o:o + n])
+            ok, err = oracle.moment_tolerance_ok(mu[k, r], ref, REL)
+            assert ok, (k, r, err)
+
+
+def test_batched_graph_replay_is_deterministic(cuda_lib):
+    from minijclsquant_gb300 import batched
+
+    datas, idxs, L, _, _ = _ensemble(5, (10, 40), seed=11)
+    B = batched.BatchedELL(datas, idxs, L)
+    v = batched.ensemble_vectors(B.rows, 2)
+    a = B.moments(200, v, dtype="c64")
+    b = B.moments(200, v, dtype="c64")
+    c = B.moments(200, v, dtype="c128")
+    d = B.moments(200, v, dtype="c128")
+    assert np.array_equal(a, b) and np.array_equal(c, d)
+    # complex64 recursion against complex128, per moment order, relative to mu_0
+    err = np.max(np.abs(a - c) / np.abs(c[:, :, :1]))
+    assert err < 5e-6
+
+
+@pytest.mark.parametrize("kernel", ["simple", "staged1"])
+def test_batched_kernel_variants_agree(cuda_lib, monkeypatch, kernel):
+    from minijclsquant_gb300 import batched
+
+    monkeypatch.setenv("KPM_STEP_KERNEL", kernel)
+    datas, idxs, L, _, _ = _ensemble(4, (30, 70), seed=5)
+    B = batched.BatchedELL(datas, idxs, L)
+    v = batched.ensemble_vectors(B.rows, 4)
+    mu = B.moments(90, v, dtype="c128")
+    for k in range(4):
+        o, n = int(B.offsets[k]), int(B.rows[k])
+        ref = oracle.rec_A_tab(90, datas[k], idxs[k], L, v[2, o:o + n])
+        assert oracle.moment_tolerance_ok(mu[k, 2], ref, REL)[0], k
+
+
+def test_batched_rejects_column_outside_its_instance(cuda_lib):
+    from minijclsquant_gb300 import _capi, batched
+
+    datas, idxs, L, _, _ = _ensemble(3, (4, 6), seed=1)
+    bad = [i.copy() for i in idxs]
+    bad[1][0] = datas[1].size // L  # one past the instance's last row (a valid row of the stack)
+    with pytest.raises(_capi.KPMError) as e:
+        batched.BatchedELL(datas, bad, L)
+    assert e.value.status == _capi.KPM_ERR_INDEX
+
+
+def test_batched_dos_per_instance(cuda_lib):
+    """DOS of each instance from the batched moments equals the plain drop-in path."""
+    from minijclsquant_gb300 import batched, device
+
+    datas, idxs, L, bnds, _ = _ensemble(3, (12, 20), seed=8)
+    B = batched.BatchedELL(datas, idxs, L)
+    v = batched.ensemble_vectors(B.rows, 2)
+    mu = B.moments(64, v, dtype="c128")
+    dos = batched.batched_dos(mu, bnds, 64)
+    for k in range(3):
+        o, n = int(B.offsets[k]), int(B.rows[k])
+        op = device.DeviceELL(datas[k], idxs[k], L)
+        mk = device.cheb_moments(op, 64, v[:, o:o + n])
+        from minijclsquant_gb300.observables import dos_from_moments
+
+        ref = dos_from_moments(mk, bnds[k], 64)
+        assert np.max(np.abs(dos[k][:, 1] - ref[:, 1])) <= 1e-10 * np.max(np.abs(ref[:, 1]))

@@ -221,6 +221,36 @@ def test_long_recursion_crosses_moment_chunks(cuda_lib):
         assert oracle.moment_tolerance_ok(mu, ref, REL)[0], M
 
 
+@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2"])
+@pytest.mark.parametrize("dtype,R", [("c128", 8), ("c128", 1), ("c128", 4), ("c64", 2), ("c64", 8), ("c64", 1)])
+def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R):
+    """Each recursion-step kernel the autotuner can pick, forced, against the oracle
+    (complex128 at 1e-10; complex64 at its own precision)."""
+    from minijclsquant_gb300 import _capi, device, lattice
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    monkeypatch.setenv("KPM_STEP_KERNEL", kernel)
+    H = lattice.honeycomb(40, 36, t=-2.7, W=0.7, seed=5)  # 2880 sites: several tiles, ragged last CTA
+    Hk = H.modifier(modifier_bounds)
+    op = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row)
+    n = op.n
+    vs = np.stack([random_vector_generator(n, 40 + r) for r in range(R)])
+    mu = device.cheb_moments(op, 150, vs, dtype=dtype)
+    kind, U = ctypes.c_int(), ctypes.c_int()
+    code = _capi.KPM_C128 if dtype == "c128" else _capi.KPM_C64
+    assert cuda_lib.kpm_ell_step_config(op.handle, code, R, ctypes.byref(kind), ctypes.byref(U), None, None) == 0
+    assert (kind.value, U.value) == {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2)}[kernel] or kind.value == 0
+    assert cuda_lib.kpm_ell_check(op.handle, None) == 0
+    for r in range(R):
+        ref = oracle.rec_A_tab(150, Hk.data, Hk.indices, Hk.len_row, vs[r])
+        if dtype == "c128":
+            ok, err = oracle.moment_tolerance_ok(mu[r], ref, REL)
+            assert ok, (kernel, r, err)
+        else:
+            assert np.max(np.abs(mu[r] - ref)) / n < 2e-6, (kernel, r)
+
+
 def test_larger_lattice_against_oracle(cuda_lib):
     """256 x 256 cells (131k sites), M = 160, R = 2: GPU vs oracle; properties at this size."""
     from minijclsquant_gb300 import device, lattice

@@ -118,3 +118,19 @@ def test_lattice_open_boundary_padding():
     assert np.sum(arr["valid"]) == 2 * (3 * 3 * 3 - 3 - 3)  # directed bonds of a 3x3 open flake
     assert np.all(arr["data"][arr["valid"] == 0] == 0)
     assert np.all((arr["indices"] >= 0) & (arr["indices"] < n))
+
+
+def test_honeycomb_ensemble_is_seeded_and_rescaled():
+    from minijclsquant_gb300 import batched
+
+    d1, i1, L, b1, p1 = batched.honeycomb_ensemble(5, side_range=(4, 9), seed=7)
+    d2, i2, _, b2, p2 = batched.honeycomb_ensemble(5, side_range=(4, 9), seed=7)
+    assert all(np.array_equal(x, y) for x, y in zip(d1, d2))
+    assert np.array_equal(p1["sides"], p2["sides"]) and np.all((p1["sides"] >= 4) & (p1["sides"] <= 9))
+    for d, b, s in zip(d1, b1, p1["sides"]):
+        assert d.size == 2 * s * s * L
+        # rescaled by the instance's own bound: every Gershgorin disc inside [-1/1.01, 1/1.01]
+        rows = np.abs(d.reshape(-1, L)).sum(axis=1)
+        assert rows.max() <= 1 / 1.01 + 1e-12
+    v = batched.ensemble_vectors([8, 18], 2, seed0=3)
+    assert v.shape == (2, 26) and np.allclose(np.abs(v), 1.0)

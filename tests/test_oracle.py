@@ -86,6 +86,31 @@ def test_oracle_cpu_dos_configuration():
         assert ok, err
 
 
+def test_oracle_adjoint_gradient_against_finite_differences():
+    """The FP64 adjoint oracle (the reference gradient for the GPU adjoint) is pinned by
+    central differences of the oracle's own moments, h = 1e-6."""
+    from minijclsquant_gb300 import lattice
+
+    arr = lattice.honeycomb_arrays(4, 3, t=-1.0, W=0.8, seed=2, with_geometry=False)
+    n, L = arr["n"], arr["len_row"]
+    d = arr["data"] / 4.0
+    v = np.exp(1j * np.random.default_rng(1).uniform(0, 2 * np.pi, n))
+    M = 20
+    c = np.random.default_rng(2).normal(size=M)
+
+    def loss(dd):
+        return float(np.sum(c * oracle.rec_A_tab(M, dd, arr["indices"], L, v, threads=1).real))
+
+    g = oracle.adjoint_grad(M, d, arr["indices"], L, v, c)
+    h = 1e-6
+    for q in range(0, n * L, 7):
+        dp, dm = d.copy(), d.copy()
+        dp[q] += h
+        dm[q] -= h
+        fd = (loss(dp) - loss(dm)) / (2 * h)
+        assert abs(g[q] - fd) <= 1e-7 * max(1.0, abs(fd)), (q, g[q], fd)
+
+
 @pytest.mark.skipif(not os.path.isdir("/root/reference/jclsquant"), reason="reference tree not present")
 def test_oracle_against_live_reference():
     """Fresh seeded case, run through the live reference (built from its .pyx) and the oracle."""

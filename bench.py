@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--batch-M", type=int, default=1024)
     ap.add_argument("--batch-R", type=int, default=2)
     ap.add_argument("--batch-side-max", type=int, default=512)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-DOS measurement")
+    ap.add_argument("--adj-cells", type=int, default=512)
+    ap.add_argument("--adj-M", type=int, default=1024)
     return ap.parse_args()
 
 
@@ -360,6 +363,80 @@ def run_batched(a, hbm_peak, steps, warmup):
             "gpu_launches_per_step": 2 + 1 + max(0, M - 2) + 1}
 
 
+def run_adjoint(a, steps, warmup):
+    """The differentiable DOS configuration: 512 x 512 cells (524,288 sites), learnable
+    FP64 on-site potentials U[-0.5, 0.5] eV and per-bond hoppings -2.7 + U[-0.1, 0.1] eV,
+    L2 loss against the DOS of another disorder draw on 512 energies, M = 1024, R = 4,
+    checkpoints every 32 orders.  Reports forward and forward+backward times (their
+    ratio is the adjoint cost) and the gradient against central differences
+    (h = 1e-6) on 64 seeded random parameters."""
+    import torch
+
+    from minijclsquant_gb300 import adjoint
+
+    cells, M, R = a.adj_cells, a.adj_M, 4
+    n = 2 * cells * cells
+    rng = np.random.default_rng(5)
+    on0 = rng.uniform(-0.5, 0.5, n)
+    hop0 = None
+    plan = adjoint.DosPlan(cells, cells, M=M, R=R, n_energies=512, ckpt=32, onsite0=on0)
+    hop0 = -2.7 + rng.uniform(-0.1, 0.1, plan.n_bonds)
+    onsite = torch.tensor(on0, dtype=torch.float64, device="cuda", requires_grad=True)
+    hop = torch.tensor(hop0, dtype=torch.float64, device="cuda", requires_grad=True)
+    rng_t = np.random.default_rng(6)
+    with torch.no_grad():
+        target = adjoint.kpm_dos(torch.tensor(rng_t.uniform(-0.5, 0.5, n), device="cuda"),
+                                 torch.tensor(-2.7 + rng_t.uniform(-0.1, 0.1, plan.n_bonds), device="cuda"), plan)
+
+    def fwd():
+        with torch.no_grad():
+            return adjoint.dos_l2_loss(onsite, hop, plan, target)
+
+    def fwd_bwd():
+        onsite.grad = None
+        hop.grad = None
+        loss = adjoint.dos_l2_loss(onsite, hop, plan, target)
+        loss.backward()
+        return loss
+
+    def timeit(fn, k):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / k
+
+    t_f = timeit(fwd, steps)
+    t_fb = timeit(fwd_bwd, steps)
+    go, gh = onsite.grad.detach().cpu().numpy(), hop.grad.detach().cpu().numpy()
+    pick = np.random.default_rng(7)
+    params = [("onsite", int(i)) for i in pick.choice(n, 32, replace=False)] + \
+             [("hopping", int(i)) for i in pick.choice(plan.n_bonds, 32, replace=False)]
+    h = 1e-6
+    worst = 0.0
+    scale = max(np.max(np.abs(go)), np.max(np.abs(gh)))
+    with torch.no_grad():
+        for which, i in params:
+            p = onsite if which == "onsite" else hop
+            old = p[i].item()
+            p[i] = old + h
+            lp = fwd().item()
+            p[i] = old - h
+            lm = fwd().item()
+            p[i] = old
+            fd = (lp - lm) / (2 * h)
+            an = (go if which == "onsite" else gh)[i]
+            worst = max(worst, abs(an - fd) / scale)
+    return {"workload": "differentiable DOS: %dx%d cells (%d sites), M=%d, R=%d, 512 energies, checkpoints every 32"
+                        % (cells, cells, n, M, R),
+            "forward_ms": 1e3 * t_f, "forward_backward_ms": 1e3 * t_fb, "backward_over_forward": (t_fb - t_f) / t_f,
+            "fwd_plus_bwd_over_fwd": t_fb / t_f,
+            "fd_check": {"params": len(params), "h": h, "max_abs_err_over_max_grad": worst}}
+
+
 def run_ours(a):
     import ctypes
 
@@ -484,6 +561,9 @@ def run_ours(a):
         del op, v
         torch.cuda.empty_cache()
         line["batched_c64"] = run_batched(a, hbm_peak, a.steps, a.warmup)
+    if not a.no_adjoint:
+        torch.cuda.empty_cache()
+        line["adjoint"] = run_adjoint(a, a.steps, a.warmup)
     if rank == 0 and world == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(prob, a.cpu_seconds)
     if rank == 0:

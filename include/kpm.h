@@ -44,6 +44,7 @@ extern "C" {
 #define KPM_ERR_INDEX 7         /* an ELL column index is outside [0, n)      */
 #define KPM_ERR_UNSUPPORTED 8   /* valid request this build does not serve    */
 #define KPM_ERR_NONFINITE 9     /* a moment came out NaN or Inf               */
+#define KPM_ERR_TOO_LARGE 10    /* beyond the fixed scratch of kpm_cheb_moments_noalloc */
 
 /* ---- precision selectors ----------------------------------------------- */
 #define KPM_C128 0   /* complex128 recursion, FP64 moments (the drop-in form)   */
@@ -184,6 +185,28 @@ int kpm_batch_info(const kpm_batch* b, int* n_inst, int64_t* rows_total, int64_t
 int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, double* mu,
                       void* stream);
 int kpm_batch_check(kpm_batch* b, void* stream);
+
+/* ---- moments without any device allocation --------------------------------
+ * No counterpart in the reference.  For callers that may not allocate device
+ * memory: a plugin inside a host application that owns the whole device
+ * budget, or code between latency-critical launches where cudaMalloc /
+ * cudaFree (which can synchronise the device) are not allowed.  Such callers
+ * cannot create a kpm_ell handle, which allocates.
+ * mu[m] = <v | T_m(H) v>, m < M, for ONE vector, with H given directly as the
+ * caller's device arrays in jclsquant's padded row-major ELL layout
+ * (data: n*len_row c128, indices: n*len_row int32, already rescaled).
+ * v: device [n] c128; mu: device [M] c128.  Nothing is allocated: the working
+ * vectors and moment partials live in one fixed file-scope device array
+ * (about 33 MiB, held by every GPU that loads the library until exit), so
+ * n <= 1,048,576 sites; larger n returns KPM_ERR_TOO_LARGE.
+ * The first call on a device looks up that array's address (once per
+ * device): make it outside any stream capture.  All calls on a device share
+ * the array: calls that overlap on the GPU race; serialise them.  The call
+ * waits for its stream to finish so it can return KPM_ERR_INDEX when a column
+ * index is outside [0, n) (such entries are skipped).
+ */
+int kpm_cheb_moments_noalloc(const double* data, const int32_t* indices, int len_row, int64_t n,
+                             const double* v, int M, double* mu, void* stream);
 
 /* ---- reference-compatible host-pointer entry points ---------------------
  * Same names and argument lists as jclsquant/cuda_cython/cuda/obv.h:21-23,30,

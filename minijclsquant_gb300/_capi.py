@@ -21,6 +21,7 @@ KPM_ERR_TIMEOUT = 6
 KPM_ERR_INDEX = 7
 KPM_ERR_UNSUPPORTED = 8
 KPM_ERR_NONFINITE = 9
+KPM_ERR_TOO_LARGE = 10
 
 KPM_C128 = 0
 KPM_C64 = 1
@@ -58,6 +59,7 @@ SIGNATURES = {
     "kpm_ell_set_values": (_I, [_P, _P, _U, _P]),
     "kpm_adjoint_forward": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "kpm_adjoint_backward": (_I, [_P, _P, _P, _P]),
+    "kpm_cheb_moments_noalloc": (_I, [_P, _P, _I, _I64, _P, _I, _P, _P]),
     "kpm_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _P, _P, _P]),
     "kpm_batch_destroy": (_I, [_P]),
     "kpm_batch_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),

@@ -283,6 +283,7 @@ const char* kpm_strerror(int status) {
     case KPM_ERR_INDEX: return "ELL column index out of range";
     case KPM_ERR_UNSUPPORTED: return "unsupported request";
     case KPM_ERR_NONFINITE: return "non-finite value";
+    case KPM_ERR_TOO_LARGE: return "larger than the fixed scratch of the no-allocation entry point";
     default: return "unknown status";
   }
 }

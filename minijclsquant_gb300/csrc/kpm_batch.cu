@@ -34,6 +34,21 @@ struct kpm_batch_s {
   };
   std::vector<G> graphs;
   DevBuf mu_int;                       // internal moments [n_inst][R][M]
+  // partial-slot layout per (precision, R)
+  struct Plan {
+    int f32 = 0, R = 0;
+    int tile_first = 0;                // grid-stride tile (first step)
+    int64_t ntiles_first = 0;
+    int64_t* d_ibeg_first = nullptr;   // [n_inst + 1] tile ranges of the first step
+    int kind = 0, U = 1, grid = 0, tile = 0;
+    int64_t nslots = 0;                // partial slots per later step
+    int64_t* d_ibeg = nullptr;         // [n_inst + 1] slot ranges of later steps
+    bool own_ibeg = false;
+    int* d_tile_inst = nullptr;        // staged: instance of each tile
+    int* d_seg_base = nullptr;         // staged: first slot of each CTA
+    int chunk = 2;
+  };
+  std::vector<Plan> plans;
 };
 
 namespace {
@@ -112,14 +127,14 @@ __global__ void batch_pack_kernel(const double2* __restrict__ src, const int64_t
   }
 }
 
-// part[step][tile][R] -> mu[k][r][m0 + step], tiles of instance k = [poff_k/TILE, (poff_k + npad_k)/TILE)
-__global__ void batch_reduce_kernel(const double2* __restrict__ part, int64_t ntiles, int tile_rows,
-                                    const int64_t* __restrict__ poff, int64_t n_pad, int n_inst, int R,
-                                    double2* __restrict__ mu, int M, int m0) {
+// part[step][slot][R] -> mu[k][r][m0 + step]; instance k owns slots [ibeg[k], ibeg[k+1]).
+// One CTA per (r, instance, step); fixed-order strided sums and a fixed tree.
+__global__ void batch_reduce_kernel(const double2* __restrict__ part, int64_t nslots,
+                                    const int64_t* __restrict__ ibeg, int R, double2* __restrict__ mu, int M,
+                                    int m0) {
   const int r = blockIdx.x, k = blockIdx.y, step = blockIdx.z;
-  const int64_t t0 = poff[k] / tile_rows;
-  const int64_t t1 = (k + 1 < n_inst ? poff[k + 1] : n_pad) / tile_rows;
-  const double2* base = part + (int64_t)step * ntiles * R;
+  const int64_t t0 = ibeg[k], t1 = ibeg[k + 1];
+  const double2* base = part + (int64_t)step * nslots * R;
   double sr = 0.0, si = 0.0;
   for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
     const double2 v = base[t * R + r];
@@ -149,23 +164,105 @@ int check_cuda(cudaError_t e) {
   return e == cudaErrorMemoryAllocation ? KPM_ERR_OOM : KPM_ERR_CUDA;
 }
 
-// Steps whose per-tile partials are buffered before a segmented reduction.
-int batch_chunk(int64_t ntiles, int R) {
-  const int64_t per_step = ntiles * R * (int64_t)sizeof(double2);
+// Steps whose partials are buffered before a segmented reduction.
+int batch_chunk(int64_t nslots, int R) {
+  const int64_t per_step = nslots * R * (int64_t)sizeof(double2);
   int64_t c = ((int64_t)256 << 20) / std::max<int64_t>(1, per_step);
   return (int)std::max<int64_t>(2, std::min<int64_t>(c, kChunk));
 }
 
+int upload(void** dst, const void* src, size_t bytes) {
+  int rc = check_cuda(cudaMalloc(dst, bytes));
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+  return rc;
+}
+
+// Build (or find) the partial-slot layout of a batched recursion for (precision, R):
+// the first step runs the grid-stride kernel with one CTA per tile (slots = tiles);
+// later steps run the staged kernel with contiguous tile ranges per CTA (slots =
+// (CTA, instance) runs), or the grid-stride kernel again when the staged one cannot.
+int batch_plan(kpm_batch_s* b, bool f32, int R, const kpm_batch_s::Plan** out) {
+  for (auto& pl : b->plans)
+    if (pl.f32 == (int)f32 && pl.R == R) {
+      *out = &pl;
+      return KPM_OK;
+    }
+  kpm_ell_s* h = b->op;
+  kpm_batch_s::Plan pl;
+  pl.f32 = (int)f32;
+  pl.R = R;
+  pl.tile_first = kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
+  pl.ntiles_first = h->n_pad / pl.tile_first;
+  std::vector<int64_t> ib(b->n_inst + 1);
+  for (int k = 0; k < b->n_inst; ++k) ib[k] = b->poff[k] / pl.tile_first;
+  ib[b->n_inst] = pl.ntiles_first;
+  KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_ibeg_first), ib.data(), ib.size() * sizeof(int64_t)));
+  const char* force = getenv("KPM_STEP_KERNEL");
+  const bool simple_only = force && std::string(force) == "simple";
+  int U = 0, occ = 0;
+  for (int u = 2; u >= 1 && !simple_only; --u) {
+    occ = f32 ? staged_ctas_f32(h->is_real, R, u, h->L, 2) : staged_ctas_f64(h->is_real, R, u, h->L, 2);
+    if (occ > 0) {
+      U = u;
+      break;
+    }
+  }
+  if (U == 0) {  // grid-stride kernel, one CTA per tile
+    pl.kind = 0;
+    pl.tile = pl.tile_first;
+    pl.grid = (int)pl.ntiles_first;
+    pl.nslots = pl.ntiles_first;
+    pl.d_ibeg = pl.d_ibeg_first;
+    pl.own_ibeg = false;
+  } else {
+    pl.kind = 1;
+    pl.U = U;
+    pl.tile = staged_tile_rows(f32, R, U);
+    const int64_t ntiles = h->n_pad / pl.tile;
+    pl.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
+    std::vector<int> tinst(ntiles);
+    for (int k = 0; k < b->n_inst; ++k) {
+      const int64_t t0 = b->poff[k] / pl.tile;
+      const int64_t t1 = (k + 1 < b->n_inst ? b->poff[k + 1] : h->n_pad) / pl.tile;
+      for (int64_t t = t0; t < t1; ++t) tinst[t] = k;
+    }
+    std::vector<int> seg_base(pl.grid);
+    std::vector<int64_t> ibeg(b->n_inst + 1, -1);
+    int64_t slot = 0;
+    for (int g = 0; g < pl.grid; ++g) {
+      const int64_t tb = ((int64_t)g * ntiles) / pl.grid, te = ((int64_t)(g + 1) * ntiles) / pl.grid;
+      seg_base[g] = (int)slot;
+      for (int64_t t = tb; t < te; ++t)
+        if (t == tb || tinst[t] != tinst[t - 1]) {
+          if (ibeg[tinst[t]] < 0) ibeg[tinst[t]] = slot;
+          ++slot;
+        }
+    }
+    ibeg[b->n_inst] = slot;
+    pl.nslots = slot;
+    KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_tile_inst), tinst.data(), tinst.size() * sizeof(int)));
+    KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_seg_base), seg_base.data(), seg_base.size() * sizeof(int)));
+    KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_ibeg), ibeg.data(), ibeg.size() * sizeof(int64_t)));
+    pl.own_ibeg = true;
+  }
+  pl.chunk = batch_chunk(pl.nslots, R);
+  b->plans.push_back(pl);
+  *out = &b->plans.back();
+  return KPM_OK;
+}
+
+// Partial-buffer elements (double2) a plan needs: two first-step blocks, then chunk NEXT blocks.
+int64_t plan_part_elems(const kpm_batch_s::Plan& pl, int R) {
+  return 2 * pl.ntiles_first * R + (int64_t)pl.chunk * pl.nslots * R;
+}
+
 // The launch sequence of one batched recursion on internal buffers:
-// ta = T_0 (packed), tb = T_1, vl = left vectors, part = per-tile partials,
-// mu_int = [n_inst][R][M].
-int record_batched(kpm_batch_s* b, bool f32, int R, int M, const StepConfig& cfg, cudaStream_t s) {
+// ta = T_0 (packed), tb = T_1, vl = left vectors, part = partials, mu_int = [n_inst][R][M].
+int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Plan& pl, cudaStream_t s) {
   kpm_ell_s* h = b->op;
   Workspace& ws = h->ws;
-  const int tile = cfg.kind == 1 ? staged_tile_rows(f32, R, 1) : kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
-  const int64_t ntiles = h->n_pad / tile;
-  const int chunk = batch_chunk(ntiles, R);
-  double2* part = static_cast<double2*>(ws.part.p);
+  double2* part_first = static_cast<double2*>(ws.part.p);
+  double2* part = part_first + 2 * pl.ntiles_first * R;
   double2* mu = static_cast<double2*>(b->mu_int.p);
   StepParams p;
   std::memset(&p, 0, sizeof(p));
@@ -177,44 +274,49 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const StepConfig& cfg
   p.a_half = make_double2(0.5, 0.0);
   p.err = h->err_flag;
   p.vl = ws.vl.p;
-  p.part_step_stride = ntiles * R;
-  // m = 1 (and mu_0): grid = one CTA per tile of the grid-stride kernel, so its per-CTA
-  // partials are per-tile partials
-  const int tile_simple = kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
-  const int64_t ntiles_simple = h->n_pad / tile_simple;
-  if (ntiles_simple != ntiles) return KPM_ERR_UNSUPPORTED;
+  // m = 1 and mu_0: one grid-stride CTA per tile, so per-CTA partials are per-tile partials
+  p.part_step_stride = pl.ntiles_first * R;
   p.tcur = ws.ta.p;
   p.tout = ws.tb.p;
-  p.part = part;
-  KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)ntiles, s)
-              : launch_step_f64(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)ntiles, s));
+  p.part = part_first;
+  KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)pl.ntiles_first, s)
+              : launch_step_f64(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)pl.ntiles_first, s));
+  {
+    dim3 g(R, b->n_inst, M >= 2 ? 2 : 1);
+    batch_reduce_kernel<<<g, 128, 0, s>>>(part_first, pl.ntiles_first, pl.d_ibeg_first, R, mu, M, 0);
+    KPM_CUDA_TRY(cudaGetLastError());
+  }
+  p.tile_inst = pl.d_tile_inst;
+  p.seg_base = pl.d_seg_base;
   void* tprev = ws.ta.p;
   void* tcur = ws.tb.p;
-  int m0 = 0;
+  int m0 = 2;
   for (int m = 2; m < M; ++m) {
-    if (m - m0 == chunk) {
-      dim3 g(R, b->n_inst, chunk);
-      batch_reduce_kernel<<<g, 128, 0, s>>>(part, ntiles, tile, b->d_poff, h->n_pad, b->n_inst, R, mu, M, m0);
+    if (m - m0 == pl.chunk) {
+      dim3 g(R, b->n_inst, pl.chunk);
+      batch_reduce_kernel<<<g, 128, 0, s>>>(part, pl.nslots, pl.d_ibeg, R, mu, M, m0);
       KPM_CUDA_TRY(cudaGetLastError());
       m0 = m;
     }
     p.tcur = tcur;
     p.tout = tprev;
-    p.part = part + (int64_t)(m - m0) * ntiles * R;
-    if (cfg.kind == 1) {
+    p.part = part + (int64_t)(m - m0) * pl.nslots * R;
+    if (pl.kind == 1) {
       p.per_tile = 1;
-      KPM_TRY(f32 ? launch_staged_f32(h->is_real, R, 1, p, cfg.grid, s)
-                  : launch_staged_f64(h->is_real, R, 1, p, cfg.grid, s));
+      KPM_TRY(f32 ? launch_staged_f32(h->is_real, R, pl.U, p, pl.grid, s)
+                  : launch_staged_f64(h->is_real, R, pl.U, p, pl.grid, s));
     } else {
       p.per_tile = 0;
-      KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, (int)ntiles, s)
-                  : launch_step_f64(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, (int)ntiles, s));
+      KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, pl.grid, s)
+                  : launch_step_f64(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, pl.grid, s));
     }
     std::swap(tprev, tcur);
   }
-  dim3 g(R, b->n_inst, M - m0);
-  batch_reduce_kernel<<<g, 128, 0, s>>>(part, ntiles, tile, b->d_poff, h->n_pad, b->n_inst, R, mu, M, m0);
-  KPM_CUDA_TRY(cudaGetLastError());
+  if (M > m0) {
+    dim3 g(R, b->n_inst, M - m0);
+    batch_reduce_kernel<<<g, 128, 0, s>>>(part, pl.nslots, pl.d_ibeg, R, mu, M, m0);
+    KPM_CUDA_TRY(cudaGetLastError());
+  }
   return KPM_OK;
 }
 
@@ -313,6 +415,12 @@ int kpm_batch_create(kpm_batch** out, int n_inst, const int64_t* inst_rows, int 
 int kpm_batch_destroy(kpm_batch* b) {
   if (!b) return KPM_ERR_INVALID_ARG;
   for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+  for (auto& pl : b->plans) {
+    if (pl.d_ibeg_first) cudaFree(pl.d_ibeg_first);
+    if (pl.own_ibeg && pl.d_ibeg) cudaFree(pl.d_ibeg);
+    if (pl.d_tile_inst) cudaFree(pl.d_tile_inst);
+    if (pl.d_seg_base) cudaFree(pl.d_seg_base);
+  }
   release(b->mu_int);
   if (b->d_off) cudaFree(b->d_off);
   if (b->d_poff) cudaFree(b->d_poff);
@@ -345,34 +453,10 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
   KPM_TRY(ensure(ws.tb, vb));
   KPM_TRY(ensure(ws.vl, vb));
   KPM_TRY(ensure(b->mu_int, (size_t)b->n_inst * R * M * sizeof(double2)));
-  // kernel choice: staged (one row per thread, per-tile partials) or grid-stride, timed once
-  StepConfig cfg;
-  {
-    const int key = (f32 ? 1000 : 0) + R * 10 + 9;  // batched entries are keyed apart from plain ones
-    bool found = false;
-    for (auto& kv : h->tuned)
-      if (kv.first == key) {
-        cfg = kv.second;
-        found = true;
-      }
-    if (!found) {
-      const int occ = f32 ? staged_ctas_f32(h->is_real, R, 1, h->L, 2) : staged_ctas_f64(h->is_real, R, 1, h->L, 2);
-      const int tile = staged_tile_rows(f32, R, 1);
-      const int64_t ntiles = h->n_pad / tile;
-      cfg.kind = occ > 0 ? 1 : 0;
-      cfg.U = 1;
-      cfg.grid = occ > 0 ? (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count)) : (int)ntiles;
-      const char* force = getenv("KPM_STEP_KERNEL");
-      if (force && std::string(force) == "simple") {
-        cfg.kind = 0;
-        cfg.grid = (int)ntiles;
-      }
-      h->tuned.emplace_back(key, cfg);
-    }
-  }
-  const int tile = staged_tile_rows(f32, R, 1);
-  const int64_t ntiles = h->n_pad / tile;
-  KPM_TRY(ensure(ws.part, (size_t)batch_chunk(ntiles, R) * ntiles * R * sizeof(double2)));
+  // kernel choice and partial-slot layout (built once per precision and R)
+  const kpm_batch_s::Plan* plan = nullptr;
+  KPM_TRY(batch_plan(b, f32, R, &plan));
+  KPM_TRY(ensure(ws.part, (size_t)plan_part_elems(*plan, R) * sizeof(double2)));
   // inputs into the internal buffers (outside the graph)
   batch_pack_kernel<<<grid1(h->n_pad * R), 256, 0, s>>>(reinterpret_cast<const double2*>(v), b->d_off, b->d_poff,
                                                          b->d_rows, b->n_inst, b->n_total, h->n_pad, R, f32, ws.ta.p);
@@ -383,7 +467,7 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
   cudaGraphExec_t exec = nullptr;
   for (size_t i = 0; i < b->graphs.size(); ++i) {
     auto& g = b->graphs[i];
-    if (g.f32 == (int)f32 && g.R == R && g.M == M && g.kind == cfg.kind) {
+    if (g.f32 == (int)f32 && g.R == R && g.M == M && g.kind == plan->kind) {
       if (std::equal(bufs, bufs + 5, g.bufs)) {
         exec = g.exec;
       } else {
@@ -395,14 +479,14 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
   }
   const bool use_graph = getenv("KPM_NO_GRAPH") == nullptr;
   if (!use_graph) {
-    KPM_TRY(record_batched(b, f32, R, M, cfg, s));
+    KPM_TRY(record_batched(b, f32, R, M, *plan, s));
   } else {
     if (!exec) {
       cudaStream_t cs;
       KPM_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
       cudaGraph_t graph;
       KPM_CUDA_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      const int rc = record_batched(b, f32, R, M, cfg, cs);
+      const int rc = record_batched(b, f32, R, M, *plan, cs);
       const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
       cudaStreamDestroy(cs);
       if (rc != KPM_OK) return rc;
@@ -414,7 +498,7 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
       g.f32 = (int)f32;
       g.R = R;
       g.M = M;
-      g.kind = cfg.kind;
+      g.kind = plan->kind;
       std::copy(bufs, bufs + 5, g.bufs);
       g.exec = exec;
       b->graphs.push_back(g);

@@ -119,8 +119,11 @@ struct StepParams {
   double2 a_half;         // APPLY: a/2 (values are 2H)
   double2 b;              // APPLY: b
   int* err;               // device status word (KPM_ERR_TIMEOUT from a bounded wait)
-  int per_tile;           // staged kernel: partials per tile ([sets][tiles][R]) instead of per CTA
+  int per_tile;           // staged kernel, batched operators: contiguous tile range per CTA, partials per
+                          // (CTA, instance) run at part + (seg_base[cta] + run) * R
   const void* tprev;      // grid-stride MODE_NEXT: read T_{m-1} here instead of tout (out of place)
+  const int* tile_inst;   // per_tile: instance of every tile
+  const int* seg_base;    // per_tile: first partial slot of every CTA
 };
 
 // Launch helpers implemented per precision (kpm_cheb_c128.cu, kpm_cheb_c64.cu).

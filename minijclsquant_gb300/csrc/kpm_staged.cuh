@@ -90,7 +90,14 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
   const uint32_t stage_b = col_b + val_b + 2 * vec_b;
 
   const int ntiles = (int)(p.n_pad / TILE);
-  const int my_count = ((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  // tiles of this CTA: strided (plain operators) or one contiguous range (batched)
+  const int seg_tb = (int)(((int64_t)blockIdx.x * ntiles) / gridDim.x);
+  const int seg_te = (int)(((int64_t)(blockIdx.x + 1) * ntiles) / gridDim.x);
+  const int my_count = p.per_tile ? seg_te - seg_tb
+                                  : (((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0);
+  auto tile_of = [&](int k) -> int64_t {
+    return p.per_tile ? (int64_t)seg_tb + k : (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
+  };
 
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -117,9 +124,11 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
     tc.val_b = val_b;
     tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + 2 * vec_b;
     for (int k = 0; k < kStages - 1 && k < my_count; ++k)
-      issue_tile(tc, smem + (k % kStages) * stage_b, &bars[k % kStages],
-                 ((int64_t)blockIdx.x + (int64_t)k * gridDim.x) * TILE, TPR * (int)sizeof(Raw), pol);
+      issue_tile(tc, smem + (k % kStages) * stage_b, &bars[k % kStages], tile_of(k) * TILE, TPR * (int)sizeof(Raw),
+                 pol);
   }
+  int seg = p.per_tile ? p.seg_base[blockIdx.x] : 0;
+  int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
 
   const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
   Raw* tout = static_cast<Raw*>(p.tout);
@@ -138,8 +147,8 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
     if (threadIdx.x == 0 && k + kStages - 1 < my_count) {
       fence_proxy_async_shared();
       const int kn = k + kStages - 1;
-      issue_tile(tc, smem + (kn % kStages) * stage_b, &bars[kn % kStages],
-                 ((int64_t)blockIdx.x + (int64_t)kn * gridDim.x) * TILE, TPR * (int)sizeof(Raw), pol);
+      issue_tile(tc, smem + (kn % kStages) * stage_b, &bars[kn % kStages], tile_of(kn) * TILE,
+                 TPR * (int)sizeof(Raw), pol);
     }
     const int st = k % kStages;
     const bool ok = mbar_wait_bounded(&bars[st], (uint32_t)((k / kStages) & 1));
@@ -149,7 +158,7 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
       const MV* sval = reinterpret_cast<const MV*>(base + col_b);
       const Raw* sold = reinterpret_cast<const Raw*>(base + col_b + val_b);
       const Raw* svl = reinterpret_cast<const Raw*>(base + col_b + val_b + vec_b);
-      const int64_t row0 = ((int64_t)blockIdx.x + (int64_t)k * gridDim.x) * TILE;
+      const int64_t row0 = tile_of(k) * TILE;
       Cx<T, VPT> acc[U];
       for (int s = 0; s < L; s += 4) {
         int c[U][4];
@@ -217,19 +226,24 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
       return;
     }
     if (p.per_tile) {
-      if (F32) {
+      // flush the accumulators when the next tile belongs to another instance (or at the end)
+      const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
+      if (next_inst != cur_inst) {
+        if (F32) {
 #pragma unroll
-        for (int q = 0; q < VPT; ++q) {
-          mr[q] += (double)fr[q];
-          mi[q] += (double)fi[q];
-          fr[q] = fi[q] = T(0);
+          for (int q = 0; q < VPT; ++q) {
+            mr[q] += (double)fr[q];
+            mi[q] += (double)fi[q];
+            fr[q] = fi[q] = T(0);
+          }
+          pending = 0;
         }
-        pending = 0;
-      }
-      const int64_t tile = (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
-      block_reduce_store<TPR, VPT>(mr, mi, p.part + tile * R, red);
+        block_reduce_store<TPR, VPT>(mr, mi, p.part + (int64_t)seg * R, red);
 #pragma unroll
-      for (int q = 0; q < VPT; ++q) mr[q] = mi[q] = 0.0;
+        for (int q = 0; q < VPT; ++q) mr[q] = mi[q] = 0.0;
+        ++seg;
+        cur_inst = next_inst;
+      }
     }
   }
 

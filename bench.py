@@ -347,7 +347,7 @@ def run_batched(a, hbm_peak, steps, warmup):
     dos_err = max(float(np.max(np.abs(x[:, 1] - y[:, 1])) / np.max(np.abs(y[:, 1]))) for x, y in zip(d64, d128))
     mom_err = np.abs(mu64 - mu128) / np.abs(mu128[:, :, :1])
     per_order = mom_err.max(axis=(0, 1))
-    bytes_per_site_step = L * (4 + 4) / R + 4 * 8
+    bytes_per_site_step = L * (8 + 4) / R + 4 * 8  # split-float value (8 B) + index per slot
     ach = bytes_per_site_step * val64 / 1e9
     return {"workload": "%d honeycomb instances, sides U{32..%d} cells (%d sites total), W~U[0,2] eV, R=%d, M=%d"
                         % (B.n_inst, a.batch_side_max, B.n_total, R, M),
@@ -490,7 +490,8 @@ def run_ours(a):
 
     # roofline of the dominant kernel (the fused step, MODE_NEXT)
     s_v = 16 if a.dtype == "c128" else 8
-    val_bytes = (8 if op.is_real else 16) if a.dtype == "c128" else (4 if op.is_real else 8)
+    # complex128: FP64 values; complex64: exact float pairs (hi, lo) -- 8 B real, 16 B complex either way
+    val_bytes = 8 if op.is_real else 16
     bytes_per_row = L * (val_bytes + 4) + R * 4 * s_v
     bytes_per_launch = float(n) * bytes_per_row
     avg_launch_s = (loop_ms.value * 1e-3) / max(1, launches.value)

@@ -161,6 +161,23 @@ int kpm_ell_set_values(kpm_ell* h, const double* data, unsigned flags, void* str
 int kpm_adjoint_forward(kpm_ell* h, int R, int M, int ckpt, const double* v, double* mu, void* stream);
 int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream);
 
+/* ---- Kubo-Greenwood moment matrix on the tensor cores ---------------------
+ * No counterpart in the reference (its conductivity is the time-domain
+ * correlator of for_time_sigma); velocity conventions are those of
+ * modifier_velocity (jclsquant/modifiers.py:56-79).
+ * kpm_mu_nm: mu[n][m] = (1/R) sum_r <v_r | V T_n(H) V T_m(H) | v_r>, n, m < Nm
+ *   (Nm <= 256), H and V Hermitian operators of equal size (V a second
+ *   operator, e.g. -i H o dx).  Complex64 recursions; the contraction runs on
+ *   tcgen05 tensor cores (kind::tf32, 3xTF32 split, FP32 accumulation, split-K
+ *   reduced in FP64).  v: device [R][n] c128; mu: device [Nm][Nm] c128.
+ * kpm_mu_contract: the contraction alone, mu (+)= scale * sum_k conj(L_n) R_m
+ *   for row blocks L, R of 256 complex64 vectors ([256][ld] floats, interleaved
+ *   re/im, rows >= Nm ignored), k_floats = 2 * vector length (multiple of 16),
+ *   16-byte aligned device pointers; accumulate != 0 adds into mu. */
+int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double* mu, void* stream);
+int kpm_mu_contract(const float* L, const float* R, int64_t k_floats, int64_t ld, int Nm, double scale,
+                    int accumulate, double* mu, void* stream);
+
 /* ---- batched operators ---------------------------------------------------
  * n_inst independent operators of one ELL width, stacked block-diagonally and
  * advanced by one recursion (one launch per step over all instances, the

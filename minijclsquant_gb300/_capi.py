@@ -60,6 +60,8 @@ SIGNATURES = {
     "kpm_adjoint_forward": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "kpm_adjoint_backward": (_I, [_P, _P, _P, _P]),
     "kpm_cheb_moments_noalloc": (_I, [_P, _P, _I, _I64, _P, _I, _P, _P]),
+    "kpm_mu_nm": (_I, [_P, _P, _I, _I, _P, _P, _P]),
+    "kpm_mu_contract": (_I, [_P, _P, _I64, _I64, _I, _D, _I, _P, _P]),
     "kpm_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _P, _P, _P]),
     "kpm_batch_destroy": (_I, [_P]),
     "kpm_batch_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),

@@ -401,7 +401,7 @@ int kpm_ell_info(const kpm_ell* h, int64_t* n_rows, int* len_row, int* is_real, 
   if (device_bytes) {
     int64_t slots = (int64_t)h->L * h->n_pad;
     int64_t b = slots * (h->is_real ? 8 : 16) + slots * 4;
-    if (h->val32) b += slots * (h->is_real ? 4 : 8);
+    if (h->val32) b += slots * (h->is_real ? 8 : 16);
     const Workspace& w = h->ws;
     const DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef,
                             &w.ckpt, &w.seg, &w.grad};

@@ -55,25 +55,33 @@ __device__ __forceinline__ float4 pack(const Cx<float, 2>& c) {
   return make_float4(c.re[0], c.im[0], c.re[1], c.im[1]);
 }
 
+// Operator value types.  complex128 path: double (real) or double2 (complex).
+// complex64 path: every value is carried as an exact two-float split of the FP64
+// value 2H = hi + lo (hi = fl32(2H), lo = fl32(2H - hi)): float2 {hi, lo} for a
+// real operator, float4 {re_hi, im_hi, re_lo, im_lo} for a complex one.  The
+// vectors and all arithmetic stay in FP32; the split only keeps the operator
+// itself from being perturbed by float rounding, which would shift the whole
+// spectrum (a systematic DOS error that no averaging removes).
 template <typename T, bool REAL>
 struct MatV { using type = T; };
 template <>
 struct MatV<double, false> { using type = double2; };
 template <>
-struct MatV<float, false> { using type = float2; };
+struct MatV<float, true> { using type = float2; };
+template <>
+struct MatV<float, false> { using type = float4; };
 
-// acc += h * x for a real matrix value.
-template <typename T, int VPT>
-__device__ __forceinline__ void madd(Cx<T, VPT>& acc, T h, const Cx<T, VPT>& x) {
+// acc += h * x
+template <int VPT>
+__device__ __forceinline__ void madd(Cx<double, VPT>& acc, double h, const Cx<double, VPT>& x) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     acc.re[k] = fma(h, x.re[k], acc.re[k]);
     acc.im[k] = fma(h, x.im[k], acc.im[k]);
   }
 }
-// acc += h * x for a complex matrix value.
-template <typename T, int VPT, typename C2>
-__device__ __forceinline__ void madd(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x) {
+template <int VPT>
+__device__ __forceinline__ void madd(Cx<double, VPT>& acc, double2 h, const Cx<double, VPT>& x) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     acc.re[k] = fma(h.x, x.re[k], acc.re[k]);
@@ -82,19 +90,39 @@ __device__ __forceinline__ void madd(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x)
     acc.im[k] = fma(h.y, x.re[k], acc.im[k]);
   }
 }
+template <int VPT>
+__device__ __forceinline__ void madd(Cx<float, VPT>& acc, float2 h, const Cx<float, VPT>& x) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = fmaf(h.x, x.re[k], fmaf(h.y, x.re[k], acc.re[k]));
+    acc.im[k] = fmaf(h.x, x.im[k], fmaf(h.y, x.im[k], acc.im[k]));
+  }
+}
+template <int VPT>
+__device__ __forceinline__ void madd(Cx<float, VPT>& acc, float4 h, const Cx<float, VPT>& x) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    float cr = fmaf(h.z, x.re[k], -h.w * x.im[k]);
+    float ci = fmaf(h.z, x.im[k], h.w * x.re[k]);
+    acc.re[k] = fmaf(h.x, x.re[k], fmaf(-h.y, x.im[k], acc.re[k] + cr));
+    acc.im[k] = fmaf(h.x, x.im[k], fmaf(h.y, x.re[k], acc.im[k] + ci));
+  }
+}
 
 // acc = h * x - old: the first slot of a recursion row, with -T_{m-1} folded
 // into the addend of the multiply-add (no separate negation).
-template <typename T, int VPT>
-__device__ __forceinline__ void madd_first_neg(Cx<T, VPT>& acc, T h, const Cx<T, VPT>& x, const Cx<T, VPT>& old) {
+template <int VPT>
+__device__ __forceinline__ void madd_first_neg(Cx<double, VPT>& acc, double h, const Cx<double, VPT>& x,
+                                               const Cx<double, VPT>& old) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     acc.re[k] = fma(h, x.re[k], -old.re[k]);
     acc.im[k] = fma(h, x.im[k], -old.im[k]);
   }
 }
-template <typename T, int VPT, typename C2>
-__device__ __forceinline__ void madd_first_neg(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x, const Cx<T, VPT>& old) {
+template <int VPT>
+__device__ __forceinline__ void madd_first_neg(Cx<double, VPT>& acc, double2 h, const Cx<double, VPT>& x,
+                                               const Cx<double, VPT>& old) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     acc.re[k] = fma(h.x, x.re[k], -old.re[k]);
@@ -103,22 +131,47 @@ __device__ __forceinline__ void madd_first_neg(Cx<T, VPT>& acc, C2 h, const Cx<T
     acc.im[k] = fma(h.y, x.re[k], acc.im[k]);
   }
 }
+template <int VPT>
+__device__ __forceinline__ void madd_first_neg(Cx<float, VPT>& acc, float2 h, const Cx<float, VPT>& x,
+                                               const Cx<float, VPT>& old) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = fmaf(h.x, x.re[k], fmaf(h.y, x.re[k], -old.re[k]));
+    acc.im[k] = fmaf(h.x, x.im[k], fmaf(h.y, x.im[k], -old.im[k]));
+  }
+}
+template <int VPT>
+__device__ __forceinline__ void madd_first_neg(Cx<float, VPT>& acc, float4 h, const Cx<float, VPT>& x,
+                                               const Cx<float, VPT>& old) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.re[k] = -old.re[k];
+    acc.im[k] = -old.im[k];
+  }
+  madd(acc, h, x);
+}
 // acc = h * x (first slot without a previous vector).
-template <typename T, int VPT>
-__device__ __forceinline__ void mul_first(Cx<T, VPT>& acc, T h, const Cx<T, VPT>& x) {
+template <int VPT>
+__device__ __forceinline__ void mul_first(Cx<double, VPT>& acc, double h, const Cx<double, VPT>& x) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     acc.re[k] = h * x.re[k];
     acc.im[k] = h * x.im[k];
   }
 }
-template <typename T, int VPT, typename C2>
-__device__ __forceinline__ void mul_first(Cx<T, VPT>& acc, C2 h, const Cx<T, VPT>& x) {
+template <int VPT>
+__device__ __forceinline__ void mul_first(Cx<double, VPT>& acc, double2 h, const Cx<double, VPT>& x) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
     acc.re[k] = fma(-h.y, x.im[k], h.x * x.re[k]);
     acc.im[k] = fma(h.y, x.re[k], h.x * x.im[k]);
   }
+}
+template <int VPT, typename HS>
+__device__ __forceinline__ void mul_first(Cx<float, VPT>& acc, HS h, const Cx<float, VPT>& x) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) acc.re[k] = acc.im[k] = 0.f;
+  madd(acc, h, x);
 }
 
 // conj(l) * t, accumulated into (re, im).

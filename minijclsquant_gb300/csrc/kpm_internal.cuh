@@ -4,7 +4,8 @@
 //   val64 : 2*H values, SoA [slot][n_pad]; double when every value is real,
 //           double2 (re, im) otherwise.  Doubling is exact in binary floating
 //           point, so T_{m+1} = (2H) T_m - T_{m-1} needs no extra multiply.
-//   val32 : the same values rounded to float / float2 (built on first KPM_C64 use)
+//   val32 : the same values as exact float pairs (hi, lo): float2 per real value,
+//           float4 per complex value (built on first KPM_C64 use)
 //   col   : int32 column indices, SoA [slot][n_pad]
 // Rows are padded to a multiple of kRowAlign with value 0 and column 0, so
 // every kernel runs without a bounds check in its inner loop.

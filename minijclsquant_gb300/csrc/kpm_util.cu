@@ -144,26 +144,36 @@ int reduce_partials(const double2* part, int steps, int sets, int grid, int Rg, 
 }
 
 // ---------------------------------------------------------------------------
-// Complex64 copy of the operator values (2H rounded to float; the doubling
-// stays exact).
-__global__ void values_to_f32_kernel(const double* __restrict__ src, float* __restrict__ dst, int64_t count) {
+// Complex64 form of the operator values: each FP64 value 2H (doubling exact) as an
+// exact pair of floats hi = fl32(2H), lo = fl32(2H - hi) -- float2 {hi, lo} per
+// real value, float4 {re_hi, im_hi, re_lo, im_lo} per complex value.
+__global__ void values_split_kernel(const double* __restrict__ src, int64_t count, bool cplx, void* dst) {
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count;
-       t += (int64_t)gridDim.x * blockDim.x)
-    dst[t] = (float)src[t];
+       t += (int64_t)gridDim.x * blockDim.x) {
+    if (cplx) {
+      const double re = src[2 * t], im = src[2 * t + 1];
+      const float rh = (float)re, ih = (float)im;
+      static_cast<float4*>(dst)[t] = make_float4(rh, ih, (float)(re - (double)rh), (float)(im - (double)ih));
+    } else {
+      const double v = src[t];
+      const float h = (float)v;
+      static_cast<float2*>(dst)[t] = make_float2(h, (float)(v - (double)h));
+    }
+  }
 }
 
 int ensure_f32_values(kpm_ell_s* h, cudaStream_t s) {
   if (h->val32) return KPM_OK;
-  const int64_t count = (int64_t)h->L * h->n_pad * (h->is_real ? 1 : 2);
+  const int64_t count = (int64_t)h->L * h->n_pad;  // values
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, count * sizeof(float));
+  cudaError_t e = cudaMalloc(&p, count * (h->is_real ? sizeof(float2) : sizeof(float4)));
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
     (void)cudaGetLastError();
     return KPM_ERR_OOM;
   }
-  values_to_f32_kernel<<<launch_grid_for(count), 256, 0, s>>>(static_cast<const double*>(h->val64),
-                                                              static_cast<float*>(p), count);
+  values_split_kernel<<<launch_grid_for(count), 256, 0, s>>>(static_cast<const double*>(h->val64), count,
+                                                             h->is_real == 0, p);
   e = cudaGetLastError();
   if (e != cudaSuccess) {
     cudaFree(p);

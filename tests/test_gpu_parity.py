@@ -302,8 +302,8 @@ def test_complex64_error_against_complex128(cuda_lib, case):
     d128 = dos_from_moments(z["mu"], z["bounds"], 512)
     err_dos = np.max(np.abs(d64[:, 1] - d128[:, 1])) / np.max(np.abs(d128[:, 1]))
     print("c64 max|dmu|/mu0 = %.3e  DOS error = %.3e" % (err_mom, err_dos))
-    assert err_mom < 1e-5
-    assert err_dos < 1e-5
+    assert err_mom < 1e-6
+    assert err_dos < 1e-6
 
 
 def test_bad_column_index_is_rejected(cuda_lib):

@@ -90,24 +90,88 @@ __device__ __forceinline__ void madd(Cx<double, VPT>& acc, double2 h, const Cx<d
     acc.im[k] = fma(h.y, x.re[k], acc.im[k]);
   }
 }
+// Complex64 accumulation without intermediate rounding: every product h*x is
+// split exactly (TwoProduct via FMA) and added with an exact TwoSum into a
+// (hi, lo) pair, so a recursion row T_{m+1} = 2H T_m - T_{m-1} is rounded to
+// float once, when it is stored.  The _rn intrinsics keep the compiler from
+// contracting these steps.  (Error-free transformations: T. J. Dekker,
+// Numer. Math. 18 (1971) 224; D. E. Knuth, TAOCP vol. 2, 4.2.2.)
 template <int VPT>
-__device__ __forceinline__ void madd(Cx<float, VPT>& acc, float2 h, const Cx<float, VPT>& x) {
+struct CxC {
+  Cx<float, VPT> hi, lo;
+};
+
+__device__ __forceinline__ void two_prod_add(float& hi, float& lo, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float e = __fmaf_rn(a, b, -p);
+  const float s = __fadd_rn(hi, p);
+  const float bp = __fsub_rn(s, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+  hi = s;
+  lo = __fadd_rn(lo, __fadd_rn(err, e));
+}
+
+// acc += (h.x + h.y) * x, h a real value split into float hi / lo
+template <int VPT>
+__device__ __forceinline__ void madd(CxC<VPT>& acc, float2 h, const Cx<float, VPT>& x) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    acc.re[k] = fmaf(h.x, x.re[k], fmaf(h.y, x.re[k], acc.re[k]));
-    acc.im[k] = fmaf(h.x, x.im[k], fmaf(h.y, x.im[k], acc.im[k]));
+    two_prod_add(acc.hi.re[k], acc.lo.re[k], h.x, x.re[k]);
+    two_prod_add(acc.hi.im[k], acc.lo.im[k], h.x, x.im[k]);
+    acc.lo.re[k] = __fmaf_rn(h.y, x.re[k], acc.lo.re[k]);
+    acc.lo.im[k] = __fmaf_rn(h.y, x.im[k], acc.lo.im[k]);
   }
 }
+// acc += h * x, h a complex value split as {re_hi, im_hi, re_lo, im_lo}
 template <int VPT>
-__device__ __forceinline__ void madd(Cx<float, VPT>& acc, float4 h, const Cx<float, VPT>& x) {
+__device__ __forceinline__ void madd(CxC<VPT>& acc, float4 h, const Cx<float, VPT>& x) {
 #pragma unroll
   for (int k = 0; k < VPT; ++k) {
-    float cr = fmaf(h.z, x.re[k], -h.w * x.im[k]);
-    float ci = fmaf(h.z, x.im[k], h.w * x.re[k]);
-    acc.re[k] = fmaf(h.x, x.re[k], fmaf(-h.y, x.im[k], acc.re[k] + cr));
-    acc.im[k] = fmaf(h.x, x.im[k], fmaf(h.y, x.re[k], acc.im[k] + ci));
+    two_prod_add(acc.hi.re[k], acc.lo.re[k], h.x, x.re[k]);
+    two_prod_add(acc.hi.re[k], acc.lo.re[k], -h.y, x.im[k]);
+    two_prod_add(acc.hi.im[k], acc.lo.im[k], h.x, x.im[k]);
+    two_prod_add(acc.hi.im[k], acc.lo.im[k], h.y, x.re[k]);
+    acc.lo.re[k] = __fmaf_rn(h.z, x.re[k], __fmaf_rn(-h.w, x.im[k], acc.lo.re[k]));
+    acc.lo.im[k] = __fmaf_rn(h.z, x.im[k], __fmaf_rn(h.w, x.re[k], acc.lo.im[k]));
   }
 }
+template <int VPT, typename HS>
+__device__ __forceinline__ void madd_first_neg(CxC<VPT>& acc, HS h, const Cx<float, VPT>& x,
+                                               const Cx<float, VPT>& old) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    acc.hi.re[k] = -old.re[k];
+    acc.hi.im[k] = -old.im[k];
+    acc.lo.re[k] = acc.lo.im[k] = 0.f;
+  }
+  madd(acc, h, x);
+}
+template <int VPT, typename HS>
+__device__ __forceinline__ void mul_first(CxC<VPT>& acc, HS h, const Cx<float, VPT>& x) {
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) acc.hi.re[k] = acc.hi.im[k] = acc.lo.re[k] = acc.lo.im[k] = 0.f;
+  madd(acc, h, x);
+}
+// The stored (rounded once) value of an accumulator.
+template <int VPT>
+__device__ __forceinline__ Cx<float, VPT> finish(const CxC<VPT>& a) {
+  Cx<float, VPT> r;
+#pragma unroll
+  for (int k = 0; k < VPT; ++k) {
+    r.re[k] = __fadd_rn(a.hi.re[k], a.lo.re[k]);
+    r.im[k] = __fadd_rn(a.hi.im[k], a.lo.im[k]);
+  }
+  return r;
+}
+template <typename T, int VPT>
+__device__ __forceinline__ Cx<T, VPT> finish(const Cx<T, VPT>& a) {
+  return a;
+}
+// Accumulator type: plain for complex128, compensated for complex64.
+template <typename T, int VPT>
+struct AccOf { using type = Cx<T, VPT>; };
+template <int VPT>
+struct AccOf<float, VPT> { using type = CxC<VPT>; };
 
 // acc = h * x - old: the first slot of a recursion row, with -T_{m-1} folded
 // into the addend of the multiply-add (no separate negation).
@@ -131,25 +195,6 @@ __device__ __forceinline__ void madd_first_neg(Cx<double, VPT>& acc, double2 h, 
     acc.im[k] = fma(h.y, x.re[k], acc.im[k]);
   }
 }
-template <int VPT>
-__device__ __forceinline__ void madd_first_neg(Cx<float, VPT>& acc, float2 h, const Cx<float, VPT>& x,
-                                               const Cx<float, VPT>& old) {
-#pragma unroll
-  for (int k = 0; k < VPT; ++k) {
-    acc.re[k] = fmaf(h.x, x.re[k], fmaf(h.y, x.re[k], -old.re[k]));
-    acc.im[k] = fmaf(h.x, x.im[k], fmaf(h.y, x.im[k], -old.im[k]));
-  }
-}
-template <int VPT>
-__device__ __forceinline__ void madd_first_neg(Cx<float, VPT>& acc, float4 h, const Cx<float, VPT>& x,
-                                               const Cx<float, VPT>& old) {
-#pragma unroll
-  for (int k = 0; k < VPT; ++k) {
-    acc.re[k] = -old.re[k];
-    acc.im[k] = -old.im[k];
-  }
-  madd(acc, h, x);
-}
 // acc = h * x (first slot without a previous vector).
 template <int VPT>
 __device__ __forceinline__ void mul_first(Cx<double, VPT>& acc, double h, const Cx<double, VPT>& x) {
@@ -167,13 +212,6 @@ __device__ __forceinline__ void mul_first(Cx<double, VPT>& acc, double2 h, const
     acc.im[k] = fma(h.y, x.re[k], h.x * x.im[k]);
   }
 }
-template <int VPT, typename HS>
-__device__ __forceinline__ void mul_first(Cx<float, VPT>& acc, HS h, const Cx<float, VPT>& x) {
-#pragma unroll
-  for (int k = 0; k < VPT; ++k) acc.re[k] = acc.im[k] = 0.f;
-  madd(acc, h, x);
-}
-
 // conj(l) * t, accumulated into (re, im).
 template <typename A, typename T>
 __device__ __forceinline__ void cdot_acc(A& re, A& im, T lr, T li, T tr, T ti) {
@@ -267,7 +305,7 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
   const int64_t stride = (int64_t)gridDim.x * RPB;
   for (int64_t row = (int64_t)blockIdx.x * RPB + rl; row < p.n_pad; row += stride) {
     const int64_t vi = row * TPR + sub;
-    Cx<T, VPT> acc;
+    typename AccOf<T, VPT>::type accum;
     Cx<T, VPT> old;
     if (MODE == MODE_NEXT && p.tprev != nullptr) {
       unpack(static_cast<const Raw*>(p.tprev)[vi], old);
@@ -294,16 +332,17 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
         if (s + u < L) unpack(__ldg(tcur + (int64_t)c[u] * TPR + sub), x[u]);
       if (s == 0) {
         if (MODE == MODE_NEXT)
-          madd_first_neg(acc, h[0], x[0], old);
+          madd_first_neg(accum, h[0], x[0], old);
         else
-          mul_first(acc, h[0], x[0]);
+          mul_first(accum, h[0], x[0]);
       } else {
-        madd(acc, h[0], x[0]);
+        madd(accum, h[0], x[0]);
       }
 #pragma unroll
       for (int u = 1; u < 4; ++u)
-        if (s + u < L) madd(acc, h[u], x[u]);
+        if (s + u < L) madd(accum, h[u], x[u]);
     }
+    Cx<T, VPT> acc = finish(accum);
     if (MODE == MODE_FIRST) {
 #pragma unroll
       for (int k = 0; k < VPT; ++k) {

@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
       const Raw* sold = reinterpret_cast<const Raw*>(base + col_b + val_b);
       const Raw* svl = reinterpret_cast<const Raw*>(base + col_b + val_b + vec_b);
       const int64_t row0 = tile_of(k) * TILE;
-      Cx<T, VPT> acc[U];
+      typename AccOf<T, VPT>::type accum[U];
       for (int s = 0; s < L; s += 4) {
         int c[U][4];
         MV h[U][4];
@@ -182,15 +182,18 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
           if (s == 0) {
             Cx<T, VPT> old;
             unpack(sold[(u * RPB + rl) * TPR + sub], old);
-            madd_first_neg(acc[u], h[u][0], x[u][0], old);
+            madd_first_neg(accum[u], h[u][0], x[u][0], old);
           } else {
-            madd(acc[u], h[u][0], x[u][0]);
+            madd(accum[u], h[u][0], x[u][0]);
           }
 #pragma unroll
           for (int j = 1; j < 4; ++j)
-            if (s + j < L) madd(acc[u], h[u][j], x[u][j]);
+            if (s + j < L) madd(accum[u], h[u][j], x[u][j]);
         }
       }
+      Cx<T, VPT> acc[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc[u] = finish(accum[u]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         const int lr = u * RPB + rl;

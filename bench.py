@@ -63,6 +63,10 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-DOS measurement")
     ap.add_argument("--adj-cells", type=int, default=512)
     ap.add_argument("--adj-M", type=int, default=1024)
+    ap.add_argument("--no-kubo", action="store_true", help="skip the Kubo-Greenwood mu_nm measurement")
+    ap.add_argument("--kubo-cells", type=int, default=1024)
+    ap.add_argument("--kubo-Nm", type=int, default=256)
+    ap.add_argument("--kubo-R", type=int, default=4)
     return ap.parse_args()
 
 
@@ -337,6 +341,7 @@ def run_batched(a, hbm_peak, steps, warmup):
 
     mu64, ms64 = timed("c64", steps, warmup)
     mu128, ms128 = timed("c128", 1, 1)
+    cfg64, cfg128 = B.step_config("c64", R), B.step_config("c128", R)
     mu64 = mu64.cpu().numpy()
     mu128 = mu128.cpu().numpy()
     site_steps = float(B.n_total) * R * (M - 1)
@@ -360,6 +365,7 @@ def run_batched(a, hbm_peak, steps, warmup):
             "moment_error_vs_c128": {"max_rel_mu0": float(per_order.max()),
                                      "by_order": {str(m): float(per_order[m]) for m in (1, 10, 100, 500, M - 1) if m < M}},
             "setup_s": setup_s, "graph": "one CUDA graph launch per recursion",
+            "step_kernel": {"c64": cfg64, "c128": cfg128},
             "gpu_launches_per_step": 2 + 1 + max(0, M - 2) + 1}
 
 
@@ -437,6 +443,119 @@ def run_adjoint(a, steps, warmup):
             "fd_check": {"params": len(params), "h": h, "max_abs_err_over_max_grad": worst}}
 
 
+def _fp64_mu_block(Hd, Vd, idx, L, v, sel):
+    """FP64 mu[n][m] = <v| V T_n(H) V T_m(H) |v> for n, m in `sel`, from plain torch gathers
+    on the device (complex128 ELL products): L_n = T_n(H) V v, R_m = V T_m(H) v."""
+    import torch
+
+    n = v.shape[0]
+    d = torch.from_numpy(Hd.reshape(n, L)).cuda()
+    dv = torch.from_numpy(Vd.reshape(n, L)).cuda()
+    ix = torch.from_numpy(idx.reshape(n, L).astype(np.int64)).cuda()
+
+    def mv(a, x):
+        return (a * x[ix]).sum(1)
+
+    def chebs(x0, keep):
+        out, prev, cur = {}, None, x0
+        for m in range(max(keep) + 1):
+            if m in keep:
+                out[m] = cur
+            nxt = mv(d, cur) if m == 0 else 2 * mv(d, cur) - prev
+            prev, cur = cur, nxt
+        return out
+
+    keep = set(sel)
+    vt = torch.from_numpy(v).cuda()
+    Ls = chebs(mv(dv, vt), keep)
+    Rs = {m: mv(dv, t) for m, t in chebs(vt, keep).items()}
+    Lm = torch.stack([Ls[k] for k in sel])
+    Rm = torch.stack([Rs[k] for k in sel])
+    return (Lm.conj() @ Rm.T).cpu().numpy()
+
+
+def run_kubo(a, peaks, steps, warmup):
+    """The Kubo-Greenwood configuration: honeycomb cells x cells, W = 1 eV, V_x as a second
+    ELL operator, mu_nm for Nm = 256 with R random vectors (complex64 recursions, 3xTF32
+    tensor-core contraction).  Reports the whole mu_nm time, the contraction alone
+    (tensor TFLOP/s against the TF32 dense rate, half the measured bf16 rate), and the
+    error of a 16 x 16 sub-block (n, m = 0, 17, .., 255) against an FP64 product."""
+    import torch
+
+    from minijclsquant_gb300 import _capi, device, lattice
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    cells, Nm, R = a.kubo_cells, a.kubo_Nm, a.kubo_R
+    t0 = time.perf_counter()
+    H = lattice.honeycomb(cells, cells, t=-2.7, W=1.0, seed=11)
+    Hk = H.modifier(modifier_bounds)
+    Vx = H.modifier(modifier_velocity, "x")
+    Vk = np.ascontiguousarray(Vx.data / H.bounds[1])
+    n = int(H.shape[0])
+    hop = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row)
+    vop = device.DeviceELL(Vk, Hk.indices, Hk.len_row)
+    vs = np.stack([random_vector_generator(n, 3000 + r) for r in range(R)])
+    tv = torch.from_numpy(vs).cuda()
+    mu = torch.empty((Nm, Nm), dtype=torch.complex128, device="cuda")
+    setup_s = time.perf_counter() - t0
+    lib = _capi.lib()
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+
+    def call(rr, out):
+        _capi.check(lib.kpm_mu_nm(hop.handle, vop.handle, rr, Nm, tv.data_ptr(), out.data_ptr(), sp), "kpm_mu_nm")
+
+    def timed(fn, k, w):
+        for _ in range(w):
+            fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / k
+
+    ms = timed(lambda: call(R, mu), steps, max(1, warmup // 3))
+    # the contraction alone, on operands of the same shape (256 x 2 n_pad floats per vector)
+    n_pad = ((n + 511) // 512) * 512
+    g = torch.Generator(device="cuda").manual_seed(5)
+    A = torch.randn((256, 2 * n_pad), device="cuda", generator=g, dtype=torch.float32)
+    B = torch.randn((256, 2 * n_pad), device="cuda", generator=g, dtype=torch.float32)
+    mc = torch.empty((256, 256), dtype=torch.complex128, device="cuda")
+
+    def contract():
+        _capi.check(lib.kpm_mu_contract(A.data_ptr(), B.data_ptr(), 2 * n_pad, 2 * n_pad, 256, 1.0, 0,
+                                        mc.data_ptr(), sp), "kpm_mu_contract")
+
+    ms_c = timed(contract, max(3, steps), 3)
+    del A, B
+    mma_flops = 3 * 2 * 2 * 256 * 256 * (2 * n_pad)  # 3 split products x (Re, Im) x 2 flops x N x M x K
+    tf32_peak = peaks.get("bf16_tflops", 1900.0) / 2
+    ach = mma_flops / (ms_c * 1e-3) / 1e12
+    # error of a sub-block against FP64 (vector 0 alone)
+    sel = list(range(0, 256, 17))[:16]
+    sel = [s for s in sel if s < Nm]
+    mu1 = torch.empty((Nm, Nm), dtype=torch.complex128, device="cuda")
+    call(1, mu1)
+    got = mu1.cpu().numpy()[np.ix_(sel, sel)]
+    ref = _fp64_mu_block(Hk.data, Vk, Hk.indices, Hk.len_row, vs[0], sel)
+    err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
+    rec_site_steps = float(n) * R * 3 * Nm  # L and R recursions plus the V products, per vector
+    return {"workload": "Kubo-Greenwood mu_nm: honeycomb %dx%d cells (%d sites), W=1 eV, V_x, Nm=%d, R=%d"
+                        % (cells, cells, n, Nm, R),
+            "ms_per_mu_nm": ms, "site_steps_per_s": rec_site_steps / (ms * 1e-3), "setup_s": setup_s,
+            "contraction": {"ms_per_vector": ms_c, "mma_flops_per_vector": mma_flops,
+                            "roofline": {"bound": "tensor", "achieved": ach, "peak": tf32_peak, "unit": "TFLOP/s",
+                                         "frac": ach / tf32_peak,
+                                         "peak_source": "TF32 dense = half of MEASURED_PEAKS.json bf16_tflops"},
+                            "kernel": "mu_gemm_kernel (tcgen05.mma kind::tf32, 3xTF32, TMEM accumulators)"},
+            "fp64_check": {"block": "n, m in %s, vector 0" % sel, "max_abs_err_over_max": err}}
+
+
 def run_ours(a):
     import ctypes
 
@@ -509,8 +628,9 @@ def run_ours(a):
     kind, rpt, grid, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
     _capi.check(lib.kpm_ell_step_config(op.handle, _capi.dtype_code(a.dtype), R, ctypes.byref(kind), ctypes.byref(rpt),
                                         ctypes.byref(grid), ctypes.byref(us)))
-    kname = ("cheb_next_staged_kernel (bulk-copy staged, %d row(s)/thread)" % rpt.value if kind.value == 1
-             else "cheb_step_kernel (grid-stride, MODE_NEXT STORE|MOM1)")
+    kname = {1: "cheb_next_staged_kernel (bulk-copy staged, %d row(s)/thread)" % rpt.value,
+             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value}.get(
+        kind.value, "cheb_step_kernel (grid-stride, MODE_NEXT STORE|MOM1)")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
                 "kernel": kname, "grid": grid.value,
@@ -565,6 +685,9 @@ def run_ours(a):
     if not a.no_adjoint:
         torch.cuda.empty_cache()
         line["adjoint"] = run_adjoint(a, a.steps, a.warmup)
+    if not a.no_kubo:
+        torch.cuda.empty_cache()
+        line["kubo"] = run_kubo(a, peaks, a.steps, a.warmup)
     if rank == 0 and world == 1 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(prob, a.cpu_seconds)
     if rank == 0:

@@ -87,7 +87,8 @@ int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M);
  * device (KPM_ERR_TIMEOUT if a bounded wait ran out), then clear it. */
 int kpm_ell_check(kpm_ell* h, void* stream);
 /* The recursion-step kernel chosen for (dtype, R): kind 0 = grid-stride,
- * 1 = bulk-copy staged; rows per thread per tile; CTAs; measured us per step. */
+ * 1 = bulk-copy staged, 2 = bulk-copy staged with a producer warp; rows per
+ * thread per tile; CTAs; measured us per step. */
 int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                         float* step_us);
 
@@ -201,6 +202,12 @@ int kpm_batch_info(const kpm_batch* b, int* n_inst, int64_t* rows_total, int64_t
                    int* is_real);
 int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, double* mu,
                       void* stream);
+/* The recursion-step kernel the batched autotuner chose for (dtype, R) (kind
+ * as for kpm_ell_step_config), tuning it on `stream` first if no call has yet;
+ * rows per thread, CTAs and the measured us of one step over all instances.
+ * No counterpart in the reference. */
+int kpm_batch_step_config(kpm_batch* b, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
+                          float* step_us, void* stream);
 int kpm_batch_check(kpm_batch* b, void* stream);
 
 /* ---- moments without any device allocation --------------------------------

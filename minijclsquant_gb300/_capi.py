@@ -66,6 +66,8 @@ SIGNATURES = {
     "kpm_batch_destroy": (_I, [_P]),
     "kpm_batch_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
     "kpm_batch_moments": (_I, [_P, _I, _I, _I, _P, _P, _P]),
+    "kpm_batch_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                   ctypes.POINTER(ctypes.c_float), _P]),
     "kpm_batch_check": (_I, [_P, _P]),
     "kpm_ell_profile": (_I, [_P, _I]),
     "kpm_ell_profile_read": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),

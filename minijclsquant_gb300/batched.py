@@ -70,6 +70,19 @@ class BatchedELL:
             return out
         return mu
 
+    _KINDS = {0: "grid-stride", 1: "staged", 2: "staged+producer-warp"}
+
+    def step_config(self, dtype="c64", R=2, stream=None):
+        """The recursion-step kernel the batched autotuner chose for (dtype, R):
+        dict(kind, kernel, rows_per_thread, grid, step_us); tunes it first if needed."""
+        kind, U, grid, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        s = stream if stream is not None else torch.cuda.current_stream()
+        _capi.check(_capi.lib().kpm_batch_step_config(self._h, _capi.dtype_code(dtype), int(R), ctypes.byref(kind),
+                                                      ctypes.byref(U), ctypes.byref(grid), ctypes.byref(us),
+                                                      int(s.cuda_stream)), "kpm_batch_step_config")
+        return {"kind": kind.value, "kernel": self._KINDS.get(kind.value, "?"), "rows_per_thread": U.value,
+                "grid": grid.value, "step_us": float(us.value)}
+
     def close(self):
         h = getattr(self, "_h", None)
         if h is not None and h.value:

@@ -33,6 +33,16 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
 }
 
+// One arrival (release semantics) on `bar`, no transaction bytes.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Barrier 1 among the first `threads` threads of the CTA (a multiple of 32).
+__device__ __forceinline__ void named_sync(int threads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(threads) : "memory");
+}
+
 // L2 policy for data read once per step (operator slabs, T_{m-1}, left vectors).
 __device__ __forceinline__ uint64_t l2_evict_first_policy() {
   uint64_t pol;

@@ -47,6 +47,7 @@ struct kpm_batch_s {
     int* d_tile_inst = nullptr;        // staged: instance of each tile
     int* d_seg_base = nullptr;         // staged: first slot of each CTA
     int chunk = 2;
+    float step_us = 0.f;               // tuned time of one later step
   };
   std::vector<Plan> plans;
 };
@@ -177,74 +178,186 @@ int upload(void** dst, const void* src, size_t bytes) {
   return rc;
 }
 
-// Build (or find) the partial-slot layout of a batched recursion for (precision, R):
-// the first step runs the grid-stride kernel with one CTA per tile (slots = tiles);
-// later steps run the staged kernel with contiguous tile ranges per CTA (slots =
-// (CTA, instance) runs), or the grid-stride kernel again when the staged one cannot.
-int batch_plan(kpm_batch_s* b, bool f32, int R, const kpm_batch_s::Plan** out) {
+// Slot layout of a staged plan (contiguous tile ranges per CTA): the instance
+// of every tile, the first partial slot of every CTA, and every instance's slot
+// range (one slot per (CTA, instance) run).
+int plan_layout(kpm_batch_s* b, kpm_batch_s::Plan& pl) {
+  kpm_ell_s* h = b->op;
+  const int64_t ntiles = h->n_pad / pl.tile;
+  std::vector<int> tinst(ntiles);
+  for (int k = 0; k < b->n_inst; ++k) {
+    const int64_t t0 = b->poff[k] / pl.tile;
+    const int64_t t1 = (k + 1 < b->n_inst ? b->poff[k + 1] : h->n_pad) / pl.tile;
+    for (int64_t t = t0; t < t1; ++t) tinst[t] = k;
+  }
+  std::vector<int> seg_base(pl.grid);
+  std::vector<int64_t> ibeg(b->n_inst + 1, -1);
+  int64_t slot = 0;
+  for (int g = 0; g < pl.grid; ++g) {
+    const int64_t tb = ((int64_t)g * ntiles) / pl.grid, te = ((int64_t)(g + 1) * ntiles) / pl.grid;
+    seg_base[g] = (int)slot;
+    for (int64_t t = tb; t < te; ++t)
+      if (t == tb || tinst[t] != tinst[t - 1]) {
+        if (ibeg[tinst[t]] < 0) ibeg[tinst[t]] = slot;
+        ++slot;
+      }
+  }
+  ibeg[b->n_inst] = slot;
+  pl.nslots = slot;
+  KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_tile_inst), tinst.data(), tinst.size() * sizeof(int)));
+  KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_seg_base), seg_base.data(), seg_base.size() * sizeof(int)));
+  KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_ibeg), ibeg.data(), ibeg.size() * sizeof(int64_t)));
+  pl.own_ibeg = true;
+  return KPM_OK;
+}
+
+void plan_free_layout(kpm_batch_s::Plan& pl) {
+  if (pl.own_ibeg && pl.d_ibeg) cudaFree(pl.d_ibeg);
+  if (pl.d_tile_inst) cudaFree(pl.d_tile_inst);
+  if (pl.d_seg_base) cudaFree(pl.d_seg_base);
+  pl.d_ibeg = nullptr;
+  pl.d_tile_inst = nullptr;
+  pl.d_seg_base = nullptr;
+  pl.own_ibeg = false;
+}
+
+// One MODE_NEXT launch of a plan (moment partials into slot block `part`).
+int plan_next(kpm_batch_s* b, bool f32, int R, const kpm_batch_s::Plan& pl, StepParams p, cudaStream_t s) {
+  kpm_ell_s* h = b->op;
+  p.tile_inst = pl.d_tile_inst;
+  p.seg_base = pl.d_seg_base;
+  if (pl.kind == 1) {
+    p.per_tile = 1;
+    return f32 ? launch_staged_f32(h->is_real, R, pl.U, p, pl.grid, s) : launch_staged_f64(h->is_real, R, pl.U, p, pl.grid, s);
+  }
+  if (pl.kind == 2) {
+    p.per_tile = 1;
+    return f32 ? launch_ws_f32(h->is_real, R, pl.U, p, pl.grid, s) : launch_ws_f64(h->is_real, R, pl.U, p, pl.grid, s);
+  }
+  p.per_tile = 0;
+  return f32 ? launch_step_f32(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, pl.grid, s)
+             : launch_step_f64(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, pl.grid, s);
+}
+
+StepParams batch_params(kpm_ell_s* h, bool f32) {
+  StepParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.val = f32 ? h->val32 : h->val64;
+  p.col = h->col;
+  p.ld = h->n_pad;
+  p.L = h->L;
+  p.n_pad = h->n_pad;
+  p.a_half = make_double2(0.5, 0.0);
+  p.err = h->err_flag;
+  p.vl = h->ws.vl.p;
+  return p;
+}
+
+// Build (or find) the plan of a batched recursion for (precision, R): the
+// first step runs the grid-stride kernel with one CTA per tile (slots = tiles);
+// later steps run the kernel the autotuner picks among the grid-stride kernel
+// (one CTA per tile), the staged kernel and its producer-warp form (1 or 2 rows
+// per thread, contiguous tile ranges per CTA, slots = (CTA, instance) runs).
+// Each candidate is timed on the stacked operator itself (a few launches on
+// zeroed vectors) and the fastest is kept.  KPM_STEP_KERNEL forces one
+// (simple|staged1|staged2|ws1|ws2).
+int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_s::Plan** out) {
   for (auto& pl : b->plans)
     if (pl.f32 == (int)f32 && pl.R == R) {
       *out = &pl;
       return KPM_OK;
     }
   kpm_ell_s* h = b->op;
-  kpm_batch_s::Plan pl;
-  pl.f32 = (int)f32;
-  pl.R = R;
-  pl.tile_first = kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
-  pl.ntiles_first = h->n_pad / pl.tile_first;
+  kpm_batch_s::Plan base;
+  base.f32 = (int)f32;
+  base.R = R;
+  base.tile_first = kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
+  base.ntiles_first = h->n_pad / base.tile_first;
   std::vector<int64_t> ib(b->n_inst + 1);
-  for (int k = 0; k < b->n_inst; ++k) ib[k] = b->poff[k] / pl.tile_first;
-  ib[b->n_inst] = pl.ntiles_first;
-  KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_ibeg_first), ib.data(), ib.size() * sizeof(int64_t)));
+  for (int k = 0; k < b->n_inst; ++k) ib[k] = b->poff[k] / base.tile_first;
+  ib[b->n_inst] = base.ntiles_first;
+  KPM_TRY(upload(reinterpret_cast<void**>(&base.d_ibeg_first), ib.data(), ib.size() * sizeof(int64_t)));
   const char* force = getenv("KPM_STEP_KERNEL");
-  const bool simple_only = force && std::string(force) == "simple";
-  int U = 0, occ = 0;
-  for (int u = 2; u >= 1 && !simple_only; --u) {
-    occ = f32 ? staged_ctas_f32(h->is_real, R, u, h->L, 2) : staged_ctas_f64(h->is_real, R, u, h->L, 2);
-    if (occ > 0) {
-      U = u;
-      break;
-    }
-  }
-  if (U == 0) {  // grid-stride kernel, one CTA per tile
+  const std::string f = force ? force : "";
+
+  std::vector<kpm_batch_s::Plan> cands;
+  if (f.empty() || f == "simple") {
+    kpm_batch_s::Plan pl = base;
     pl.kind = 0;
     pl.tile = pl.tile_first;
     pl.grid = (int)pl.ntiles_first;
     pl.nslots = pl.ntiles_first;
     pl.d_ibeg = pl.d_ibeg_first;
     pl.own_ibeg = false;
-  } else {
-    pl.kind = 1;
-    pl.U = U;
-    pl.tile = staged_tile_rows(f32, R, U);
-    const int64_t ntiles = h->n_pad / pl.tile;
-    pl.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
-    std::vector<int> tinst(ntiles);
-    for (int k = 0; k < b->n_inst; ++k) {
-      const int64_t t0 = b->poff[k] / pl.tile;
-      const int64_t t1 = (k + 1 < b->n_inst ? b->poff[k + 1] : h->n_pad) / pl.tile;
-      for (int64_t t = t0; t < t1; ++t) tinst[t] = k;
-    }
-    std::vector<int> seg_base(pl.grid);
-    std::vector<int64_t> ibeg(b->n_inst + 1, -1);
-    int64_t slot = 0;
-    for (int g = 0; g < pl.grid; ++g) {
-      const int64_t tb = ((int64_t)g * ntiles) / pl.grid, te = ((int64_t)(g + 1) * ntiles) / pl.grid;
-      seg_base[g] = (int)slot;
-      for (int64_t t = tb; t < te; ++t)
-        if (t == tb || tinst[t] != tinst[t - 1]) {
-          if (ibeg[tinst[t]] < 0) ibeg[tinst[t]] = slot;
-          ++slot;
-        }
-    }
-    ibeg[b->n_inst] = slot;
-    pl.nslots = slot;
-    KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_tile_inst), tinst.data(), tinst.size() * sizeof(int)));
-    KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_seg_base), seg_base.data(), seg_base.size() * sizeof(int)));
-    KPM_TRY(upload(reinterpret_cast<void**>(&pl.d_ibeg), ibeg.data(), ibeg.size() * sizeof(int64_t)));
-    pl.own_ibeg = true;
+    cands.push_back(pl);
   }
+  int rc = KPM_OK;
+  for (int kind = 1; kind <= 2 && rc == KPM_OK; ++kind)
+    for (int U = 1; U <= 2 && rc == KPM_OK; ++U) {
+      if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
+      const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, R, U, h->L, 2) : staged_ctas_f64(h->is_real, R, U, h->L, 2))
+                                : (f32 ? ws_ctas_f32(h->is_real, R, U, h->L, 2) : ws_ctas_f64(h->is_real, R, U, h->L, 2));
+      if (occ <= 0) continue;
+      kpm_batch_s::Plan pl = base;
+      pl.kind = kind;
+      pl.U = U;
+      pl.tile = staged_tile_rows(f32, R, U);
+      const int64_t ntiles = h->n_pad / pl.tile;
+      pl.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
+      rc = plan_layout(b, pl);
+      cands.push_back(pl);
+    }
+  if (cands.empty() && rc == KPM_OK) {  // a forced kernel that cannot run here: the grid-stride kernel
+    kpm_batch_s::Plan pl = base;
+    pl.kind = 0;
+    pl.tile = pl.tile_first;
+    pl.grid = (int)pl.ntiles_first;
+    pl.nslots = pl.ntiles_first;
+    pl.d_ibeg = pl.d_ibeg_first;
+    cands.push_back(pl);
+  }
+  std::vector<float> us(cands.size(), 0.f);
+  if (rc == KPM_OK && cands.size() > 1) {
+    int64_t max_slots = 0;
+    for (auto& c : cands) max_slots = std::max(max_slots, c.nslots);
+    Workspace& ws = h->ws;
+    const size_t vb = (size_t)h->n_pad * R * (f32 ? sizeof(float2) : sizeof(double2));
+    rc = ensure(ws.part, (size_t)max_slots * R * sizeof(double2));
+    if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.ta.p, 0, vb, s));
+    if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.tb.p, 0, vb, s));
+    if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.vl.p, 0, vb, s));
+    StepParams p = batch_params(h, f32);
+    p.tcur = ws.ta.p;
+    p.tout = ws.tb.p;
+    p.part = static_cast<double2*>(ws.part.p);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (rc == KPM_OK) rc = check_cuda(cudaEventCreate(&e0));
+    if (rc == KPM_OK) rc = check_cuda(cudaEventCreate(&e1));
+    const int reps = 3;
+    for (size_t i = 0; i < cands.size() && rc == KPM_OK; ++i) {
+      rc = plan_next(b, f32, R, cands[i], p, s);
+      if (rc == KPM_OK) rc = check_cuda(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps && rc == KPM_OK; ++r) rc = plan_next(b, f32, R, cands[i], p, s);
+      if (rc == KPM_OK) rc = check_cuda(cudaEventRecord(e1, s));
+      if (rc == KPM_OK) rc = check_cuda(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      if (rc == KPM_OK) rc = check_cuda(cudaEventElapsedTime(&ms, e0, e1));
+      us[i] = 1e3f * ms / reps;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+  }
+  size_t best = 0;
+  for (size_t i = 1; i < cands.size(); ++i)
+    if (us[i] < us[best]) best = i;
+  for (size_t i = 0; i < cands.size(); ++i)
+    if (i != best || rc != KPM_OK) plan_free_layout(cands[i]);
+  if (rc != KPM_OK) {
+    cudaFree(base.d_ibeg_first);
+    return rc;
+  }
+  kpm_batch_s::Plan pl = cands[best];
+  pl.step_us = us[best];
   pl.chunk = batch_chunk(pl.nslots, R);
   b->plans.push_back(pl);
   *out = &b->plans.back();
@@ -264,16 +377,7 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Pl
   double2* part_first = static_cast<double2*>(ws.part.p);
   double2* part = part_first + 2 * pl.ntiles_first * R;
   double2* mu = static_cast<double2*>(b->mu_int.p);
-  StepParams p;
-  std::memset(&p, 0, sizeof(p));
-  p.val = f32 ? h->val32 : h->val64;
-  p.col = h->col;
-  p.ld = h->n_pad;
-  p.L = h->L;
-  p.n_pad = h->n_pad;
-  p.a_half = make_double2(0.5, 0.0);
-  p.err = h->err_flag;
-  p.vl = ws.vl.p;
+  StepParams p = batch_params(h, f32);
   // m = 1 and mu_0: one grid-stride CTA per tile, so per-CTA partials are per-tile partials
   p.part_step_stride = pl.ntiles_first * R;
   p.tcur = ws.ta.p;
@@ -286,8 +390,6 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Pl
     batch_reduce_kernel<<<g, 128, 0, s>>>(part_first, pl.ntiles_first, pl.d_ibeg_first, R, mu, M, 0);
     KPM_CUDA_TRY(cudaGetLastError());
   }
-  p.tile_inst = pl.d_tile_inst;
-  p.seg_base = pl.d_seg_base;
   void* tprev = ws.ta.p;
   void* tcur = ws.tb.p;
   int m0 = 2;
@@ -301,15 +403,7 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Pl
     p.tcur = tcur;
     p.tout = tprev;
     p.part = part + (int64_t)(m - m0) * pl.nslots * R;
-    if (pl.kind == 1) {
-      p.per_tile = 1;
-      KPM_TRY(f32 ? launch_staged_f32(h->is_real, R, pl.U, p, pl.grid, s)
-                  : launch_staged_f64(h->is_real, R, pl.U, p, pl.grid, s));
-    } else {
-      p.per_tile = 0;
-      KPM_TRY(f32 ? launch_step_f32(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, pl.grid, s)
-                  : launch_step_f64(h->is_real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, pl.grid, s));
-    }
+    KPM_TRY(plan_next(b, f32, R, pl, p, s));
     std::swap(tprev, tcur);
   }
   if (M > m0) {
@@ -439,6 +533,28 @@ int kpm_batch_info(const kpm_batch* b, int* n_inst, int64_t* rows_total, int64_t
   return KPM_OK;
 }
 
+int kpm_batch_step_config(kpm_batch* b, int dtype, int R, int* kind, int* rows_per_thread, int* grid, float* step_us,
+                          void* stream) {
+  if (!b) return KPM_ERR_INVALID_ARG;
+  if (dtype != KPM_C128 && dtype != KPM_C64) return KPM_ERR_DTYPE;
+  if (R != 1 && R != 2 && R != 4 && R != 8) return KPM_ERR_UNSUPPORTED;
+  const bool f32 = dtype == KPM_C64;
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  kpm_ell_s* h = b->op;
+  if (f32) KPM_TRY(ensure_f32_values(h, s));
+  const size_t vb = (size_t)h->n_pad * R * (f32 ? sizeof(float2) : sizeof(double2));
+  KPM_TRY(ensure(h->ws.ta, vb));
+  KPM_TRY(ensure(h->ws.tb, vb));
+  KPM_TRY(ensure(h->ws.vl, vb));
+  const kpm_batch_s::Plan* plan = nullptr;
+  KPM_TRY(batch_plan(b, f32, R, s, &plan));
+  if (kind) *kind = plan->kind;
+  if (rows_per_thread) *rows_per_thread = plan->kind == 0 ? 1 : plan->U;
+  if (grid) *grid = plan->grid;
+  if (step_us) *step_us = plan->step_us;
+  return KPM_OK;
+}
+
 int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, double* mu, void* stream) {
   if (!b || !v || !mu || M < 2) return KPM_ERR_INVALID_ARG;
   if (dtype != KPM_C128 && dtype != KPM_C64) return KPM_ERR_DTYPE;
@@ -455,7 +571,7 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
   KPM_TRY(ensure(b->mu_int, (size_t)b->n_inst * R * M * sizeof(double2)));
   // kernel choice and partial-slot layout (built once per precision and R)
   const kpm_batch_s::Plan* plan = nullptr;
-  KPM_TRY(batch_plan(b, f32, R, &plan));
+  KPM_TRY(batch_plan(b, f32, R, s, &plan));
   KPM_TRY(ensure(ws.part, (size_t)plan_part_elems(*plan, R) * sizeof(double2)));
   // inputs into the internal buffers (outside the graph)
   batch_pack_kernel<<<grid1(h->n_pad * R), 256, 0, s>>>(reinterpret_cast<const double2*>(v), b->d_off, b->d_poff,

@@ -98,15 +98,17 @@ int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams&
 int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s) {
   if (cfg.kind == 1)
     return f32 ? launch_staged_f32(real, R, cfg.U, p, cfg.grid, s) : launch_staged_f64(real, R, cfg.U, p, cfg.grid, s);
+  if (cfg.kind == 2)
+    return f32 ? launch_ws_f32(real, R, cfg.U, p, cfg.grid, s) : launch_ws_f64(real, R, cfg.U, p, cfg.grid, s);
   return launch_step(f32, real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, cfg.grid, s);
 }
 
 // Choose the MODE_NEXT kernel for (precision, R group, moment sets): the
-// grid-stride kernel or the staged kernel with 1 or 2 rows per thread, each
-// with a full wave of resident CTAs.  When several fit, each is timed on the
-// operator itself (a few launches on zeroed workspace vectors) and the fastest
-// is kept for the handle's lifetime.  KPM_STEP_KERNEL=simple|staged1|staged2
-// forces one.
+// grid-stride kernel, or the staged kernel (CTA-wide barrier per tile) or its
+// producer-warp form, each with 1 or 2 rows per thread and a full wave of
+// resident CTAs.  When several fit, each is timed on the operator itself (a few
+// launches on zeroed workspace vectors) and the fastest is kept for the
+// handle's lifetime.  KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2 forces one.
 int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out) {
   const int key = (f32 ? 1000 : 0) + Rg * 10 + sets;
   for (auto& kv : h->tuned)
@@ -124,17 +126,20 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
     cands.push_back(c);
   }
   // the staged kernel serves one moment set; two-set calls use the grid-stride kernel
-  for (int U = 1; U <= 2 && sets == 1; ++U) {
-    if (!f.empty() && f != (U == 1 ? "staged1" : "staged2")) continue;
-    const int occ = f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2) : staged_ctas_f64(h->is_real, Rg, U, h->L, 2);
-    if (occ <= 0) continue;
-    const int64_t ntiles = h->n_pad / staged_tile_rows(f32, Rg, U);
-    StepConfig c;
-    c.kind = 1;
-    c.U = U;
-    c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
-    cands.push_back(c);
-  }
+  for (int kind = 1; kind <= 2 && sets == 1; ++kind)
+    for (int U = 1; U <= 2; ++U) {
+      if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
+      const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2)
+                                       : staged_ctas_f64(h->is_real, Rg, U, h->L, 2))
+                                : (f32 ? ws_ctas_f32(h->is_real, Rg, U, h->L, 2) : ws_ctas_f64(h->is_real, Rg, U, h->L, 2));
+      if (occ <= 0) continue;
+      const int64_t ntiles = h->n_pad / staged_tile_rows(f32, Rg, U);
+      StepConfig c;
+      c.kind = kind;
+      c.U = U;
+      c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
+      cands.push_back(c);
+    }
   if (cands.empty()) {  // a forced staged kernel that cannot serve this call (two moment sets)
     StepConfig c;
     c.kind = 0;

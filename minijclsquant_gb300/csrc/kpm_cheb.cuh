@@ -25,6 +25,7 @@
 
 #include <type_traits>
 
+#include "kpm_async.cuh"
 #include "kpm_internal.cuh"
 
 namespace kpm {
@@ -225,7 +226,7 @@ __device__ __forceinline__ void cdot_acc(A& re, A& im, T lr, T li, T tr, T ti) {
 // then over the warps of the CTA, and store the R totals at out[0..R).
 template <int TPR, int VPT>
 __device__ __forceinline__ void block_reduce_store(double (&re)[VPT], double (&im)[VPT], double2* out,
-                                                   double2* smem) {
+                                                   double2* smem, bool named = false) {
   constexpr int R = TPR * VPT;
 #pragma unroll
   for (int off = TPR; off < 32; off <<= 1) {
@@ -240,7 +241,8 @@ __device__ __forceinline__ void block_reduce_store(double (&re)[VPT], double (&i
 #pragma unroll
     for (int k = 0; k < VPT; ++k) smem[warp * R + lane * VPT + k] = make_double2(re[k], im[k]);
   }
-  __syncthreads();
+  // `named`: only the kBlock compute threads take part (a warp-specialised CTA)
+  if (named) named_sync(kBlock); else __syncthreads();
   if (threadIdx.x < R) {
     double2 s = make_double2(0.0, 0.0);
 #pragma unroll 1
@@ -250,7 +252,7 @@ __device__ __forceinline__ void block_reduce_store(double (&re)[VPT], double (&i
     }
     out[threadIdx.x] = s;
   }
-  __syncthreads();
+  if (named) named_sync(kBlock); else __syncthreads();
 }
 
 template <typename T, bool REAL, int TPR, int VPT, int MODE, int EPI>

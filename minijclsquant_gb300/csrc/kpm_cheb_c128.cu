@@ -1,5 +1,6 @@
 // Complex128 instantiations of the step kernels (the drop-in form).
 #include "kpm_staged.cuh"
+#include "kpm_ws.cuh"
 
 namespace kpm {
 
@@ -28,6 +29,14 @@ int launch_staged_f64(bool real, int R, int U, const StepParams& p, int grid, cu
 
 int staged_ctas_f64(bool real, int R, int U, int L, int nvec) {
   return Staged<double>::ctas_per_sm(real, R, U, L, nvec);
+}
+
+int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+  return Ws<double>::launch(real, R, U, p, grid, s);
+}
+
+int ws_ctas_f64(bool real, int R, int U, int L, int nvec) {
+  return Ws<double>::ctas_per_sm(real, R, U, L, nvec);
 }
 
 }  // namespace kpm

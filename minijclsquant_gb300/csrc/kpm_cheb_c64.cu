@@ -2,6 +2,7 @@
 // vectors and values, FP64 moment accumulation).  Two complex64 values per
 // thread make every access a 16-byte vector load.
 #include "kpm_staged.cuh"
+#include "kpm_ws.cuh"
 
 namespace kpm {
 
@@ -30,6 +31,14 @@ int launch_staged_f32(bool real, int R, int U, const StepParams& p, int grid, cu
 
 int staged_ctas_f32(bool real, int R, int U, int L, int nvec) {
   return Staged<float>::ctas_per_sm(real, R, U, L, nvec);
+}
+
+int launch_ws_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+  return Ws<float>::launch(real, R, U, p, grid, s);
+}
+
+int ws_ctas_f32(bool real, int R, int U, int L, int nvec) {
+  return Ws<float>::ctas_per_sm(real, R, U, L, nvec);
 }
 
 }  // namespace kpm

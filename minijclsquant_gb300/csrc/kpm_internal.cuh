@@ -67,7 +67,7 @@ struct Workspace {
 
 // Kernel choice for the recursion step of one (precision, R group, moment sets).
 struct StepConfig {
-  int kind = 0;  // 0: grid-stride kernel, 1: bulk-copy staged kernel
+  int kind = 0;  // 0: grid-stride kernel, 1: bulk-copy staged kernel, 2: staged with a producer warp
   int U = 1;     // rows per thread per tile (staged)
   int grid = 0;  // CTAs
   float us = 0;  // measured time of one step launch when tuned
@@ -138,6 +138,11 @@ int launch_staged_f64(bool real, int R, int U, const StepParams& p, int grid, cu
 int launch_staged_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
 int staged_ctas_f64(bool real, int R, int U, int L, int nvec);
 int staged_ctas_f32(bool real, int R, int U, int L, int nvec);
+// The same step with a producer warp and full/empty stage barriers (kpm_ws.cuh).
+int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
+int launch_ws_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
+int ws_ctas_f64(bool real, int R, int U, int L, int nvec);
+int ws_ctas_f32(bool real, int R, int U, int L, int nvec);
 // Driver helpers (kpm_capi.cu).
 int pow2_group(int remaining);
 int vpt_for(bool f32, int Rg);

@@ -1,0 +1,326 @@
+// kpm_ws.cuh -- the staged recursion step with a producer warp.
+//
+//   T_{m+1} = 2H T_m - T_{m-1}  (in place over T_{m-1})  and  <v_l | T_{m+1}>
+//
+// Same tile layout and per-tile bulk copies as the staged kernel, but the CTA is
+// split into kBlock compute threads and one producer warp.  Each of the
+// kWsStages shared-memory stages has a "full" mbarrier (the producer's
+// expect_tx, completed by the copies) and an "empty" mbarrier (one arrival per
+// compute warp once it has read the stage).  Compute warps never meet at a
+// CTA-wide barrier inside the tile loop, so while one warp waits on its
+// neighbour gathers T_m[col] the others compute, and the producer refills a
+// stage as soon as the last warp has left it.
+//
+// Moment partials follow the staged kernel: per CTA (strided tiles) or, for
+// batched operators (per_tile), flushed per (CTA, instance) run with a block
+// reduction over the compute warps alone (named barrier 1).
+//
+// Every wait is bounded.  A compute warp whose wait runs out records
+// KPM_ERR_TIMEOUT and stops computing but still takes part in the named
+// barriers, so no warp waits on one that has left; the producer that times
+// out stops issuing and waits (bounded) for its copies in flight before exit.
+#pragma once
+
+#include "kpm_staged.cuh"
+
+namespace kpm {
+
+constexpr int kWsStages = 4;
+constexpr int kWsThreads = kBlock + 32;  // compute warps + one producer warp
+
+template <typename T, bool REAL, int TPR, int VPT, int U>
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_kernel(const StepParams p) {
+  using Raw = typename RawT<T, VPT>::type;
+  using MV = typename MatV<T, REAL>::type;
+  constexpr int R = TPR * VPT;
+  constexpr int RPB = kBlock / TPR;
+  constexpr int TILE = RPB * U;
+  constexpr bool F32 = std::is_same<T, float>::value;
+  constexpr int kFlush = 8;
+  constexpr int kWarps = kBlock / 32;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[kWsStages];
+  __shared__ __align__(8) uint64_t empty[kWsStages];
+  __shared__ double2 red[kWarps * R];
+
+  const int L = p.L;
+  const uint32_t col_b = (uint32_t)align16((size_t)L * TILE * 4);
+  const uint32_t val_b = (uint32_t)align16((size_t)L * TILE * sizeof(MV));
+  const uint32_t vec_b = (uint32_t)(TILE * TPR * sizeof(Raw));
+  const uint32_t stage_b = col_b + val_b + 2 * vec_b;
+
+  const int ntiles = (int)(p.n_pad / TILE);
+  const int seg_tb = (int)(((int64_t)blockIdx.x * ntiles) / gridDim.x);
+  const int seg_te = (int)(((int64_t)(blockIdx.x + 1) * ntiles) / gridDim.x);
+  const int my_count = p.per_tile ? seg_te - seg_tb
+                                  : (((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0);
+  auto tile_of = [&](int k) -> int64_t {
+    return p.per_tile ? (int64_t)seg_tb + k : (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
+  };
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < kWsStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kWarps);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == kWarps) {  // producer
+    if (lane == 0 && my_count > 0) {
+      TileCopy tc;
+      const uint64_t pol = l2_evict_first_policy();
+      tc.col = p.col;
+      tc.val = static_cast<const unsigned char*>(p.val);
+      tc.old = static_cast<const unsigned char*>(p.tout);
+      tc.vl = static_cast<const unsigned char*>(p.vl);
+      tc.vl2 = nullptr;
+      tc.ld = p.ld;
+      tc.L = L;
+      tc.col_slab = TILE * 4;
+      tc.val_slab = (uint32_t)(TILE * sizeof(MV));
+      tc.vec_slab = vec_b;
+      tc.col_b = col_b;
+      tc.val_b = val_b;
+      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + 2 * vec_b;
+      int issued = 0;
+      for (int k = 0; k < my_count; ++k) {
+        const int st = k % kWsStages;
+        if (k >= kWsStages && !mbar_wait_bounded(&empty[st], (uint32_t)(((k / kWsStages) - 1) & 1))) {
+          atomicExch(p.err, KPM_ERR_TIMEOUT);
+          break;
+        }
+        fence_proxy_async_shared();
+        issue_tile(tc, smem + st * stage_b, &full[st], tile_of(k) * TILE, TPR * (int)sizeof(Raw), pol);
+        issued = k + 1;
+      }
+      // copies of the last stages may still be landing: wait for them before leaving
+      for (int q = issued > kWsStages ? issued - kWsStages : 0; q < issued; ++q)
+        (void)mbar_wait_bounded(&full[q % kWsStages], (uint32_t)((q / kWsStages) & 1));
+    }
+    return;
+  }
+
+  int seg = p.per_tile ? p.seg_base[blockIdx.x] : 0;
+  int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
+
+  const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
+  Raw* tout = static_cast<Raw*>(p.tout);
+  const int sub = threadIdx.x % TPR;
+  const int rl = threadIdx.x / TPR;
+  double mr[VPT], mi[VPT];
+  T fr[VPT], fi[VPT];
+#pragma unroll
+  for (int q = 0; q < VPT; ++q) {
+    mr[q] = mi[q] = 0.0;
+    fr[q] = fi[q] = T(0);
+  }
+  int pending = 0;
+  bool dead = false;
+
+  for (int k = 0; k < my_count; ++k) {
+    const int st = k % kWsStages;
+    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / kWsStages) & 1));
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok && !dead) {
+      if (lane == 0) atomicExch(p.err, KPM_ERR_TIMEOUT);
+      dead = true;
+    }
+    if (ok) {
+      const unsigned char* base = smem + st * stage_b;
+      const int32_t* scol = reinterpret_cast<const int32_t*>(base);
+      const MV* sval = reinterpret_cast<const MV*>(base + col_b);
+      const Raw* sold = reinterpret_cast<const Raw*>(base + col_b + val_b);
+      const Raw* svl = reinterpret_cast<const Raw*>(base + col_b + val_b + vec_b);
+      const int64_t row0 = tile_of(k) * TILE;
+      typename AccOf<T, VPT>::type accum[U];
+      for (int s = 0; s < L; s += 4) {
+        int c[U][4];
+        MV h[U][4];
+        Cx<T, VPT> x[U][4];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (s + j < L) {
+              c[u][j] = scol[(s + j) * TILE + u * RPB + rl];
+              h[u][j] = sval[(s + j) * TILE + u * RPB + rl];
+            }
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (s + j < L) unpack(__ldg(tcur + (int64_t)c[u][j] * TPR + sub), x[u][j]);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          if (s == 0) {
+            Cx<T, VPT> old;
+            unpack(sold[(u * RPB + rl) * TPR + sub], old);
+            madd_first_neg(accum[u], h[u][0], x[u][0], old);
+          } else {
+            madd(accum[u], h[u][0], x[u][0]);
+          }
+#pragma unroll
+          for (int j = 1; j < 4; ++j)
+            if (s + j < L) madd(accum[u], h[u][j], x[u][j]);
+        }
+      }
+      Cx<T, VPT> acc[U], l[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        acc[u] = finish(accum[u]);
+        unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
+      }
+      // the stage is no longer read: hand it back to the producer
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        tout[(row0 + u * RPB + rl) * TPR + sub] = pack(acc[u]);
+#pragma unroll
+        for (int q = 0; q < VPT; ++q) {
+          if (F32)
+            cdot_acc(fr[q], fi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+          else
+            cdot_acc(mr[q], mi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+        }
+        if (F32 && ++pending == kFlush) {
+          pending = 0;
+#pragma unroll
+          for (int q = 0; q < VPT; ++q) {
+            mr[q] += (double)fr[q];
+            mi[q] += (double)fi[q];
+            fr[q] = fi[q] = T(0);
+          }
+        }
+      }
+    }
+    if (p.per_tile) {
+      const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
+      if (next_inst != cur_inst) {
+        if (F32) {
+#pragma unroll
+          for (int q = 0; q < VPT; ++q) {
+            mr[q] += (double)fr[q];
+            mi[q] += (double)fi[q];
+            fr[q] = fi[q] = T(0);
+          }
+          pending = 0;
+        }
+        block_reduce_store<TPR, VPT>(mr, mi, p.part + (int64_t)seg * R, red, true);
+#pragma unroll
+        for (int q = 0; q < VPT; ++q) mr[q] = mi[q] = 0.0;
+        ++seg;
+        cur_inst = next_inst;
+      }
+    }
+  }
+
+  if (!p.per_tile) {
+    if (F32) {
+#pragma unroll
+      for (int q = 0; q < VPT; ++q) {
+        mr[q] += (double)fr[q];
+        mi[q] += (double)fi[q];
+      }
+    }
+    block_reduce_store<TPR, VPT>(mr, mi, p.part + (int64_t)blockIdx.x * R, red, true);
+  }
+}
+
+template <typename T, bool REAL, int TPR, int VPT, int U>
+bool ws_smem_attr(size_t smem) {
+  static size_t configured = 0;
+  if (smem <= configured) return true;
+  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    (void)cudaGetLastError();
+    return false;
+  }
+  configured = smem;
+  return true;
+}
+
+template <typename T, bool REAL, int TPR, int VPT, int U>
+int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
+  const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U>(smem)) return KPM_ERR_UNSUPPORTED;
+  cheb_next_ws_kernel<T, REAL, TPR, VPT, U><<<grid, kWsThreads, smem, s>>>(p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return KPM_ERR_CUDA;
+  }
+  return KPM_OK;
+}
+
+template <typename T, bool REAL, int TPR, int VPT, int U>
+int ws_ctas_per_sm(int L, int nvec) {
+  const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
+  if (smem > 200 * 1024) return 0;
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U>(smem)) return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U>, kWsThreads,
+                                                    smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+// Dispatch over (real, R, U) for one precision (VPT as in the staged kernel).
+template <typename T>
+struct Ws {
+  template <bool REAL, int R, int U>
+  static int go(const StepParams& p, int grid, cudaStream_t s) {
+    constexpr int VPT = (std::is_same<T, float>::value && R >= 2) ? 2 : 1;
+    return launch_ws<T, REAL, R / VPT, VPT, U>(p, grid, s);
+  }
+  template <bool REAL, int R, int U>
+  static int occ(int L, int nvec) {
+    constexpr int VPT = (std::is_same<T, float>::value && R >= 2) ? 2 : 1;
+    return ws_ctas_per_sm<T, REAL, R / VPT, VPT, U>(L, nvec);
+  }
+  template <bool REAL, int R>
+  static int go_u(int U, const StepParams& p, int grid, cudaStream_t s) {
+    return U == 2 ? go<REAL, R, 2>(p, grid, s) : go<REAL, R, 1>(p, grid, s);
+  }
+  template <bool REAL, int R>
+  static int occ_u(int U, int L, int nvec) {
+    return U == 2 ? occ<REAL, R, 2>(L, nvec) : occ<REAL, R, 1>(L, nvec);
+  }
+  template <bool REAL>
+  static int go_r(int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+    switch (R) {
+      case 1: return go_u<REAL, 1>(U, p, grid, s);
+      case 2: return go_u<REAL, 2>(U, p, grid, s);
+      case 4: return go_u<REAL, 4>(U, p, grid, s);
+      case 8: return go_u<REAL, 8>(U, p, grid, s);
+      default: return KPM_ERR_UNSUPPORTED;
+    }
+  }
+  template <bool REAL>
+  static int occ_r(int R, int U, int L, int nvec) {
+    switch (R) {
+      case 1: return occ_u<REAL, 1>(U, L, nvec);
+      case 2: return occ_u<REAL, 2>(U, L, nvec);
+      case 4: return occ_u<REAL, 4>(U, L, nvec);
+      case 8: return occ_u<REAL, 8>(U, L, nvec);
+      default: return 0;
+    }
+  }
+  static int launch(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+    return real ? go_r<true>(R, U, p, grid, s) : go_r<false>(R, U, p, grid, s);
+  }
+  static int ctas_per_sm(bool real, int R, int U, int L, int nvec) {
+    return real ? occ_r<true>(R, U, L, nvec) : occ_r<false>(R, U, L, nvec);
+  }
+};
+
+}  // namespace kpm

@@ -53,19 +53,45 @@ def test_batched_graph_replay_is_deterministic(cuda_lib):
     assert err < 5e-6
 
 
-@pytest.mark.parametrize("kernel", ["simple", "staged1"])
-def test_batched_kernel_variants_agree(cuda_lib, monkeypatch, kernel):
+KINDS = {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2), "ws1": (2, 1), "ws2": (2, 2)}
+
+
+@pytest.mark.parametrize("kernel", list(KINDS))
+@pytest.mark.parametrize("dtype,R", [("c128", 4), ("c64", 2), ("c64", 8)])
+def test_batched_kernel_variants_agree(cuda_lib, monkeypatch, kernel, dtype, R):
+    """Every kernel the batched autotuner can pick, forced, against the oracle per
+    instance (complex128 at 1e-10 per order; complex64 at its own precision)."""
     from minijclsquant_gb300 import batched
 
     monkeypatch.setenv("KPM_STEP_KERNEL", kernel)
-    datas, idxs, L, _, _ = _ensemble(4, (30, 70), seed=5)
+    datas, idxs, L, _, _ = _ensemble(6, (3, 70), seed=5)  # 18 .. 9800 sites: tiny and multi-tile instances
     B = batched.BatchedELL(datas, idxs, L)
-    v = batched.ensemble_vectors(B.rows, 4)
-    mu = B.moments(90, v, dtype="c128")
-    for k in range(4):
+    v = batched.ensemble_vectors(B.rows, R)
+    mu = B.moments(90, v, dtype=dtype)
+    cfg = B.step_config(dtype, R)
+    assert (cfg["kind"], cfg["rows_per_thread"]) == KINDS[kernel] or cfg["kind"] == 0, cfg
+    for k in range(6):
         o, n = int(B.offsets[k]), int(B.rows[k])
-        ref = oracle.rec_A_tab(90, datas[k], idxs[k], L, v[2, o:o + n])
-        assert oracle.moment_tolerance_ok(mu[k, 2], ref, REL)[0], k
+        for r in range(R):
+            ref = oracle.rec_A_tab(90, datas[k], idxs[k], L, v[r, o:o + n])
+            if dtype == "c128":
+                assert oracle.moment_tolerance_ok(mu[k, r], ref, REL)[0], (k, r)
+            else:
+                assert np.max(np.abs(mu[k, r] - ref)) / n < 2e-6, (k, r)
+
+
+def test_batched_autotuner_reports_its_choice(cuda_lib):
+    from minijclsquant_gb300 import batched
+
+    datas, idxs, L, _, _ = _ensemble(5, (20, 60), seed=9)
+    B = batched.BatchedELL(datas, idxs, L)
+    cfg = B.step_config("c64", 2)
+    assert cfg["kind"] in (0, 1, 2) and cfg["grid"] >= 1 and cfg["step_us"] > 0
+    v = batched.ensemble_vectors(B.rows, 2)
+    a = B.moments(64, v, dtype="c64")
+    assert B.step_config("c64", 2) == cfg  # the plan is kept
+    b = B.moments(64, v, dtype="c64")
+    assert np.array_equal(a, b)
 
 
 def test_batched_rejects_column_outside_its_instance(cuda_lib):

@@ -221,7 +221,7 @@ def test_long_recursion_crosses_moment_chunks(cuda_lib):
         assert oracle.moment_tolerance_ok(mu, ref, REL)[0], M
 
 
-@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2"])
+@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2", "ws1", "ws2"])
 @pytest.mark.parametrize("dtype,R", [("c128", 8), ("c128", 1), ("c128", 4), ("c64", 2), ("c64", 8), ("c64", 1)])
 def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R):
     """Each recursion-step kernel the autotuner can pick, forced, against the oracle
@@ -240,7 +240,8 @@ def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R):
     kind, U = ctypes.c_int(), ctypes.c_int()
     code = _capi.KPM_C128 if dtype == "c128" else _capi.KPM_C64
     assert cuda_lib.kpm_ell_step_config(op.handle, code, R, ctypes.byref(kind), ctypes.byref(U), None, None) == 0
-    assert (kind.value, U.value) == {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2)}[kernel] or kind.value == 0
+    assert (kind.value, U.value) == {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2), "ws1": (2, 1),
+                                     "ws2": (2, 2)}[kernel] or kind.value == 0
     assert cuda_lib.kpm_ell_check(op.handle, None) == 0
     for r in range(R):
         ref = oracle.rec_A_tab(150, Hk.data, Hk.indices, Hk.len_row, vs[r])

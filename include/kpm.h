@@ -168,8 +168,9 @@ int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream
  * modifier_velocity (jclsquant/modifiers.py:56-79).
  * kpm_mu_nm: mu[n][m] = (1/R) sum_r <v_r | V T_n(H) V T_m(H) | v_r>, n, m < Nm
  *   (Nm <= 256), H and V Hermitian operators of equal size (V a second
- *   operator, e.g. -i H o dx).  Complex64 recursions; the contraction runs on
- *   tcgen05 tensor cores (kind::tf32, 3xTF32 split, FP32 accumulation, split-K
+ *   operator, e.g. -i H o dx).  Complex64 recursions over groups of up to 4
+ *   vectors (the workspace holds 2 x 256 rows of 2 x group x n floats: 34 GB
+ *   at n = 2.1M, group 4); the contraction runs on tcgen05 tensor cores (kind::tf32, 3xTF32 split, FP32 accumulation, split-K
  *   reduced in FP64).  v: device [R][n] c128; mu: device [Nm][Nm] c128.
  * kpm_mu_contract: the contraction alone, mu (+)= scale * sum_k conj(L_n) R_m
  *   for row blocks L, R of 256 complex64 vectors ([256][ld] floats, interleaved

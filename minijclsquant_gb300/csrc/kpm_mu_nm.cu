@@ -4,9 +4,10 @@
 //
 // computed as mu_nm = (1/R) sum_r L_n^H R_m with L_n = T_n(H) (V v) and
 // R_m = V T_m(H) v (H and V Hermitian).  The recursions run in complex64 with the
-// step kernels of this library and store every L_n and R_m as a row of a
-// [256][2 n_pad] float matrix (interleaved re, im).  The contraction is one real
-// GEMM per half of the n range,
+// step kernels of this library, up to kMuGroup vectors at once, and store every
+// L_n and R_m as a row of a [256][2 Rg n_pad] float matrix (the packed [n_pad][Rg]
+// vector set, interleaved re, im): the contraction over a row sums over sites
+// and the group's vectors alike.  It is one real GEMM per half of the n range,
 //
 //   Re mu[n][m] = sum_k A[n][k] B[m][k],   Im mu[n][m] = sum_k A'[n][k] B[m][k],
 //
@@ -28,18 +29,22 @@
 
 namespace kpm {
 
-constexpr int kTM = 128;                      // A rows (n) per CTA
-constexpr int kTN = 256;                      // B rows (m) = MMA N
-constexpr int kKt = 16;                       // tf32 K elements per stage
-constexpr int kGemmThreads = 256;
-constexpr uint32_t kLBO = 128;                // bytes between K-adjacent core matrices
-constexpr uint32_t kSBO = (kKt / 4) * 128;    // bytes between 8-row groups (512)
-constexpr uint32_t kTileA = kTM * kKt * 4;    // 8 KB
-constexpr uint32_t kTileB = kTN * kKt * 4;    // 16 KB
-constexpr uint32_t kStageBytes = 4 * kTileA + 2 * kTileB;  // Ahi Alo A'hi A'lo Bhi Blo = 64 KB
-constexpr int kGemmStages = 2;
-constexpr uint32_t kGemmSmem = kGemmStages * kStageBytes;  // 128 KB
-constexpr uint32_t kTmemCols = 512;
+constexpr int kTile = 128;                     // n rows and m rows of one output tile
+constexpr int kKt = 16;                        // tf32 K elements per stage
+constexpr int kGemmThreads = 512;                         // one A and one B chunk per thread per K tile
+constexpr int kColsPerThread = 2 * kTile * kTile / kGemmThreads;  // 64 accumulator columns of one TMEM lane
+constexpr uint32_t kLBO = 128;                 // bytes between K-adjacent core matrices
+constexpr uint32_t kSBO = (kKt / 4) * 128;     // bytes between 8-row groups (512)
+constexpr uint32_t kTileA = kTile * kKt * 4;   // 8 KB: 128 rows x 16 floats
+constexpr uint32_t kTileBX = 2 * kTileA;       // 16 KB: 128 B rows, then the same rows swapped
+constexpr uint32_t kStageBytes = 2 * kTileA + 2 * kTileBX;  // Ahi Alo BXhi BXlo = 48 KB
+constexpr int kGemmStages = 3;
+constexpr uint32_t kGemmSmem = kGemmStages * kStageBytes;  // 144 KB
+constexpr uint32_t kTmemCols = 512;            // two accumulator buffers of 256 columns (Re | Im)
+constexpr int kChainTiles = 2;                 // K tiles per TMEM accumulation chain (32 floats)
+constexpr int kLevel1Chains = 64;              // chains summed in registers before a global flush
+constexpr int kMuGroup = 4;                    // vectors per recursion group of kpm_mu_nm
+constexpr int kTileElems = kTile * kTile;
 
 struct GemmParams {
   const float* A;   // [256][lda]
@@ -47,7 +52,9 @@ struct GemmParams {
   int64_t lda;      // floats per row
   int64_t K;        // floats of K to contract (multiple of kKt)
   int64_t k_per_cta;
-  float* part;      // [KS][256][512]
+  int mt;           // m tiles (output tile index = n_tile * mt + m_tile)
+  float* part_hi;   // [KS][tiles][Re, Im][128 m][128 n]: float-float partial sums
+  float* part_lo;
   int* err;
 };
 
@@ -56,29 +63,60 @@ __device__ __forceinline__ uint32_t chunk_off(int r, int kc) {
   return (uint32_t)(r >> 3) * kSBO + (uint32_t)kc * kLBO + (uint32_t)(r & 7) * 16;
 }
 
+// The 16-byte chunk a thread moves: chunk c (0..511) of a 128-row x 16-float tile
+// is row ((c >> 5) << 3 | (c & 7)), k-chunk ((c >> 3) & 3), so the eight threads of
+// a shared-memory store phase write one 128-byte core-matrix column (no bank
+// conflicts) and a warp still reads whole 32-byte sectors of 8 rows.
+__device__ __forceinline__ int chunk_row(int c) { return ((c >> 5) << 3) | (c & 7); }
+__device__ __forceinline__ int chunk_kc(int c) { return (c >> 3) & 3; }
+
 __device__ __forceinline__ float4 tf32x4(float4 x) {
   return make_float4(to_tf32(x.x), to_tf32(x.y), to_tf32(x.z), to_tf32(x.w));
 }
 
+// One CTA: output tile (n0.., m0..) of 128 x 128, Re and Im side by side as one
+// M = 128, N = 256 MMA against BX = [B rows; B rows with (re, im) -> (im, -re)],
+// over its K range.  The MMA accumulator is restarted every kChainTiles K tiles,
+// alternating between two TMEM buffers: while one chain runs, the threads fold
+// the previous one into FP32 register sums (every thread owns one TMEM lane and
+// kColsPerThread columns), and every kLevel1Chains chains those sums go into a float-float
+// (hi, lo) partial in global memory.  The tensor core's FP32 accumulation thus
+// never runs longer than 3 * 2 * kChainTiles MMAs.
 __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmParams p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[kGemmStages];
+  __shared__ __align__(8) uint64_t accbar[2];
   __shared__ uint32_t tmem_slot;
 
-  const int n0 = blockIdx.x * kTM;
+  const int tile = blockIdx.x;
+  const int n0 = (tile / p.mt) * kTile, m0 = (tile % p.mt) * kTile;
   const int64_t k_begin = (int64_t)blockIdx.y * p.k_per_cta;
   const int64_t k_end = min(p.K, k_begin + p.k_per_cta);
   const int k_tiles = k_end > k_begin ? (int)((k_end - k_begin) / kKt) : 0;
-  float* out = p.part + ((int64_t)blockIdx.y * 256 + n0) * 512;
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
+  // TMEM lane quarter (warp % 4) and this thread's block of accumulator columns:
+  // buffer columns cb .. cb + kColsPerThread - 1 (Re: 0..127, Im: 128..255)
+  const int q = warp & 3;
+  const int cb = (warp >> 2) * kColsPerThread;
+  const int half = cb / kTile;
+  const int row = 32 * q + lane;
+  const int64_t obase = (((int64_t)blockIdx.y * gridDim.x + tile) * 2 + half) * kTileElems +
+                        (int64_t)(cb % kTile) * kTile + row;
+  float* ohi = p.part_hi + obase;  // element (column cb + c) at ohi[c * kTile]
+  float* olo = p.part_lo + obase;
 
   if (k_tiles == 0) {  // nothing to contract: a zero partial
-    for (int i = tid; i < kTM * 512; i += kGemmThreads) out[(int64_t)(i / 512) * 512 + (i % 512)] = 0.f;
+    for (int c = 0; c < kColsPerThread; ++c) {
+      ohi[c * kTile] = 0.f;
+      olo[c * kTile] = 0.f;
+    }
     return;
   }
   if (tid == 0) {
     for (int s = 0; s < kGemmStages; ++s) mbar_init(&bars[s], 1);
+    mbar_init(&accbar[0], 1);
+    mbar_init(&accbar[1], 1);
     fence_mbar_init();
   }
   if (warp == 0) {
@@ -90,122 +128,170 @@ __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmPara
   tc_fence_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t smem_base = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
-  const uint32_t idesc = idesc_tf32(kTM, kTN);
+  const uint32_t idesc = idesc_tf32(kTile, 2 * kTile);
 
-  // this thread's chunks of a tile: A 2 x 16 B, B 4 x 16 B
-  float4 ra[2], rb[4];
-  auto load_tile = [&](int t) {
-    const int64_t k0 = k_begin + (int64_t)t * kKt;
+  float run[kColsPerThread];  // level-1 sums of this thread's lane and columns
 #pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const int c = tid + kGemmThreads * i;
-      ra[i] = __ldcs(reinterpret_cast<const float4*>(p.A + (int64_t)(n0 + (c >> 2)) * p.lda + k0) + (c & 3));
-    }
+  for (int i = 0; i < kColsPerThread; ++i) run[i] = 0.f;
+  bool first_flush = true;
+  int chains_in_l1 = 0;
+
+  // fold chain c (TMEM buffer c & 1) into run[]; false if its commit never came
+  auto fold_chain = [&](int c) -> bool {
+    bool ok = mbar_wait_bounded(&accbar[c & 1], (uint32_t)((c >> 1) & 1));
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok) return false;
+    tc_fence_after();
+    const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((c & 1) * 256 + cb);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int c = tid + kGemmThreads * i;
-      rb[i] = __ldcs(reinterpret_cast<const float4*>(p.B + (int64_t)(c >> 2) * p.lda + k0) + (c & 3));
+    for (int g = 0; g < kColsPerThread / 16; ++g) {
+      float v[16];
+      tmem_ld16(base + (uint32_t)(g * 16), v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) run[g * 16 + i] = __fadd_rn(run[g * 16 + i], v[i]);
     }
+    return true;
   };
-  load_tile(0);
-  bool ok = true;
-  for (int t = 0; t < k_tiles; ++t) {
+  // level-1 sums into the float-float partial (TwoSum), then restart them
+  auto flush_l2 = [&]() {
+#pragma unroll
+    for (int c = 0; c < kColsPerThread; ++c) {
+      if (first_flush) {
+        ohi[c * kTile] = run[c];
+        olo[c * kTile] = 0.f;
+      } else {
+        const float a = ohi[c * kTile], b = run[c];
+        const float s = __fadd_rn(a, b);
+        const float bp = __fsub_rn(s, a);
+        const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+        ohi[c * kTile] = s;
+        olo[c * kTile] = __fadd_rn(olo[c * kTile], e);
+      }
+      run[c] = 0.f;
+    }
+    first_flush = false;
+  };
+
+  // this thread's 16-byte chunks of one K tile: chunk tid of the A rows and of the B rows
+  struct RawTile {
+    float4 a, b;
+  };
+  const int crow = chunk_row(tid), ckc = chunk_kc(tid);
+  const uint32_t off = chunk_off(crow, ckc);
+  const uint32_t offs = chunk_off(kTile + crow, ckc);
+  const float* pa = p.A + (int64_t)(n0 + crow) * p.lda + k_begin + 4 * ckc;
+  const float* pb = p.B + (int64_t)(m0 + crow) * p.lda + k_begin + 4 * ckc;
+  auto load_tile = [&](int t, RawTile& r) {
+    r.a = __ldcs(reinterpret_cast<const float4*>(pa + (int64_t)t * kKt));
+    r.b = __ldcs(reinterpret_cast<const float4*>(pb + (int64_t)t * kKt));
+  };
+  int issued = 0;  // K tiles whose MMAs thread 0 has issued
+  // one K tile: fold a finished chain when a new one starts, split r into the stage,
+  // prefetch tile t + 2 into r, then thread 0 issues the tile's MMAs
+  auto body = [&](int t, RawTile& r) -> bool {
     const int st = t % kGemmStages;
-    if (t >= kGemmStages) ok = mbar_wait_bounded(&bars[st], (uint32_t)(((t - kGemmStages) / kGemmStages) & 1));
-    if (__syncthreads_or(!ok)) break;
-    unsigned char* stage = smem + (size_t)st * kStageBytes;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-      const int c = tid + kGemmThreads * i;
-      const uint32_t off = chunk_off(c >> 2, c & 3);
-      const float4 x = ra[i];
-      const float4 hi = tf32x4(x);
-      const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
-      *reinterpret_cast<float4*>(stage + 0 * kTileA + off) = hi;
-      *reinterpret_cast<float4*>(stage + 1 * kTileA + off) = lo;
-      *reinterpret_cast<float4*>(stage + 2 * kTileA + off) = make_float4(-hi.y, hi.x, -hi.w, hi.z);
-      *reinterpret_cast<float4*>(stage + 3 * kTileA + off) = make_float4(-lo.y, lo.x, -lo.w, lo.z);
+    const int c = t / kChainTiles;
+    bool good = true;
+    if (t % kChainTiles == 0 && c >= 2) {  // chain c - 2 used the buffer chain c starts
+      good = fold_chain(c - 2);
+      if (good && ++chains_in_l1 == kLevel1Chains) {
+        flush_l2();
+        chains_in_l1 = 0;
+      }
     }
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      const int c = tid + kGemmThreads * i;
-      const uint32_t off = chunk_off(c >> 2, c & 3);
-      const float4 x = rb[i];
-      const float4 hi = tf32x4(x);
-      const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
-      *reinterpret_cast<float4*>(stage + 4 * kTileA + off) = hi;
-      *reinterpret_cast<float4*>(stage + 4 * kTileA + kTileB + off) = lo;
+    if (good && t >= kGemmStages)
+      good = mbar_wait_bounded(&bars[st], (uint32_t)(((t - kGemmStages) / kGemmStages) & 1));
+    if (good) {
+      unsigned char* stage = smem + (size_t)st * kStageBytes;
+      {
+        const float4 x = r.a;
+        const float4 hi = tf32x4(x);
+        const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
+        *reinterpret_cast<float4*>(stage + off) = hi;
+        *reinterpret_cast<float4*>(stage + kTileA + off) = lo;
+      }
+      {
+        const float4 x = r.b;
+        const float4 hi = tf32x4(x);
+        const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
+        unsigned char* bx = stage + 2 * kTileA;
+        *reinterpret_cast<float4*>(bx + off) = hi;
+        *reinterpret_cast<float4*>(bx + kTileBX + off) = lo;
+        *reinterpret_cast<float4*>(bx + offs) = make_float4(hi.y, -hi.x, hi.w, -hi.z);
+        *reinterpret_cast<float4*>(bx + kTileBX + offs) = make_float4(lo.y, -lo.x, lo.w, -lo.z);
+      }
     }
-    if (t + 1 < k_tiles) load_tile(t + 1);
+    if (t + 2 < k_tiles) load_tile(t + 2, r);
     fence_proxy_async_shared();
-    __syncthreads();
+    tc_fence_before();
+    if (__syncthreads_or(!good)) return false;
     if (tid == 0) {
       tc_fence_after();
       const uint32_t s0 = smem_base + (uint32_t)st * kStageBytes;
+      const uint32_t d = tmem + (uint32_t)((c & 1) * 256);
 #pragma unroll
       for (int j = 0; j < kKt / 8; ++j) {
         const uint32_t kofs = (uint32_t)j * 2 * kLBO;
-        const uint64_t a_hi = smem_desc(s0 + 0 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t a_lo = smem_desc(s0 + 1 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t ap_hi = smem_desc(s0 + 2 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t ap_lo = smem_desc(s0 + 3 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t b_hi = smem_desc(s0 + 4 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t b_lo = smem_desc(s0 + 4 * kTileA + kTileB + kofs, kLBO, kSBO);
-        const bool acc = (t > 0) || (j > 0);
-        mma_tf32(tmem + 0, a_hi, b_hi, idesc, acc);
-        mma_tf32(tmem + 0, a_hi, b_lo, idesc, true);
-        mma_tf32(tmem + 0, a_lo, b_hi, idesc, true);
-        mma_tf32(tmem + 256, ap_hi, b_hi, idesc, acc);
-        mma_tf32(tmem + 256, ap_hi, b_lo, idesc, true);
-        mma_tf32(tmem + 256, ap_lo, b_hi, idesc, true);
+        const uint64_t a_hi = smem_desc(s0 + kofs, kLBO, kSBO);
+        const uint64_t a_lo = smem_desc(s0 + kTileA + kofs, kLBO, kSBO);
+        const uint64_t bx_hi = smem_desc(s0 + 2 * kTileA + kofs, kLBO, kSBO);
+        const uint64_t bx_lo = smem_desc(s0 + 2 * kTileA + kTileBX + kofs, kLBO, kSBO);
+        mma_tf32(d, a_hi, bx_hi, idesc, (t % kChainTiles) != 0 || j > 0);
+        mma_tf32(d, a_hi, bx_lo, idesc, true);
+        mma_tf32(d, a_lo, bx_hi, idesc, true);
       }
       mma_commit(&bars[st]);
+      if ((t + 1) % kChainTiles == 0 || t + 1 == k_tiles) mma_commit(&accbar[c & 1]);
+      issued = t + 1;
     }
+    return true;
+  };
+
+  RawTile r0, r1;
+  load_tile(0, r0);
+  if (k_tiles > 1) load_tile(1, r1);
+  bool ok = true;
+  for (int t = 0; t < k_tiles && ok; t += 2) {
+    ok = body(t, r0);
+    if (ok && t + 1 < k_tiles) ok = body(t + 1, r1);
   }
-  // all MMAs issued so far are tracked by the last commit
-  const int last = k_tiles - 1;
-  if (ok) ok = mbar_wait_bounded(&bars[last % kGemmStages], (uint32_t)((last / kGemmStages) & 1));
-  if (__syncthreads_or(!ok)) {
+  if (ok) {  // the last one or two chains
+    const int nchains = (k_tiles + kChainTiles - 1) / kChainTiles;
+    bool good = true;
+    for (int c = max(0, nchains - 2); c < nchains && good; ++c) good = fold_chain(c);
+    ok = !__syncthreads_or(!good);
+  }
+  if (!ok) {
     if (tid == 0) {
       atomicExch(p.err, KPM_ERR_TIMEOUT);
-      // wait (bounded) for the MMAs still in flight before the accumulator is released
-      for (int q = max(0, last - kGemmStages + 1); q <= last; ++q)
-        (void)mbar_wait_bounded(&bars[q % kGemmStages], (uint32_t)((q / kGemmStages) & 1));
+      // the last commit tracks every MMA issued: wait (bounded) before the accumulator is released
+      if (issued > 0)
+        (void)mbar_wait_bounded(&bars[(issued - 1) % kGemmStages], (uint32_t)(((issued - 1) / kGemmStages) & 1));
     }
+    tc_fence_before();
     __syncthreads();
     if (warp == 0) tmem_dealloc(tmem, kTmemCols);
     return;
   }
-  tc_fence_after();
-  // epilogue: warp w reads TMEM lanes 32*(w%4).. and the Re (w < 4) or Im (w >= 4) columns
-  {
-    const int q = warp & 3, half = warp >> 2;
-    const int row = 32 * q + lane;
-    float* orow = out + (int64_t)row * 512 + half * 256;
-    for (int c = 0; c < 256 / 16; ++c) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(half * 256 + c * 16), v);
-#pragma unroll
-      for (int i = 0; i < 16; i += 4)
-        *reinterpret_cast<float4*>(orow + c * 16 + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
-    }
-  }
+  flush_l2();
   tc_fence_before();
   __syncthreads();
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
-// mu[n][m] = (accumulate ? mu : 0) + scale * sum_ks (part re, part im), FP64.
-__global__ void mu_reduce_kernel(const float* __restrict__ part, int KS, int Nm, double scale, int accumulate,
-                                 double2* __restrict__ mu) {
+// mu[n][m] = (accumulate ? mu : 0) + scale * sum_ks (hi + lo), Re and Im, in FP64.
+__global__ void mu_reduce_kernel(const float* __restrict__ hi, const float* __restrict__ lo, int KS, int tiles,
+                                 int mt, int Nm, double scale, int accumulate, double2* __restrict__ mu) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= Nm * Nm) return;
   const int n = idx / Nm, m = idx % Nm;
+  const int tile = (n / kTile) * mt + (m / kTile);
+  const int64_t off = (int64_t)(m % kTile) * kTile + (n % kTile);
   double re = 0.0, im = 0.0;
   for (int ks = 0; ks < KS; ++ks) {
-    const float* row = part + ((int64_t)ks * 256 + n) * 512;
-    re += (double)row[m];
-    im += (double)row[256 + m];
+    const int64_t b = ((int64_t)ks * tiles + tile) * 2 * kTileElems + off;
+    re += (double)hi[b] + (double)lo[b];
+    im += (double)hi[b + kTileElems] + (double)lo[b + kTileElems];
   }
   double2 o = make_double2(scale * re, scale * im);
   if (accumulate) {
@@ -215,6 +301,20 @@ __global__ void mu_reduce_kernel(const float* __restrict__ part, int KS, int Nm,
   mu[idx] = o;
 }
 
+int mu_tiles(int Nm) {
+  const int t = (Nm + kTile - 1) / kTile;
+  return t * t;
+}
+
+int contract_splits(int64_t K, int sm_count, int tiles) {
+  int64_t ks = std::max<int64_t>(1, sm_count / tiles);
+  ks = std::min<int64_t>(ks, K / kKt);
+  return (int)std::max<int64_t>(1, ks);
+}
+
+// Floats of the partial buffer (hi and lo planes).
+size_t contract_part_floats(int KS, int tiles) { return (size_t)2 * KS * tiles * 2 * kTileElems; }
+
 int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, double scale, int accumulate,
                 double2* mu, float* part, int KS, int* err, cudaStream_t s) {
   static bool attr = false;
@@ -222,6 +322,8 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
     KPM_CUDA_TRY(cudaFuncSetAttribute(mu_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
     attr = true;
   }
+  const int mt = (Nm + kTile - 1) / kTile;
+  const int tiles = mt * mt;
   GemmParams g;
   g.A = A;
   g.B = B;
@@ -229,19 +331,16 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
   g.K = K;
   g.k_per_cta = ((K / KS + kKt - 1) / kKt) * kKt;
   if (g.k_per_cta < kKt) g.k_per_cta = kKt;
-  g.part = part;
+  g.mt = mt;
+  g.part_hi = part;
+  g.part_lo = part + (size_t)KS * tiles * 2 * kTileElems;
   g.err = err;
-  mu_gemm_kernel<<<dim3(2, KS), kGemmThreads, kGemmSmem, s>>>(g);
+  mu_gemm_kernel<<<dim3(tiles, KS), kGemmThreads, kGemmSmem, s>>>(g);
   KPM_CUDA_TRY(cudaGetLastError());
-  mu_reduce_kernel<<<(Nm * Nm + 255) / 256, 256, 0, s>>>(part, KS, Nm, scale, accumulate, mu);
+  mu_reduce_kernel<<<(Nm * Nm + 255) / 256, 256, 0, s>>>(g.part_hi, g.part_lo, KS, tiles, mt, Nm, scale, accumulate,
+                                                         mu);
   KPM_CUDA_TRY(cudaGetLastError());
   return KPM_OK;
-}
-
-int contract_splits(int64_t K, int sm_count) {
-  int64_t ks = std::max<int64_t>(1, sm_count / 2);
-  ks = std::min<int64_t>(ks, K / kKt);
-  return (int)std::max<int64_t>(1, ks);
 }
 
 }  // namespace kpm
@@ -259,10 +358,10 @@ int kpm_mu_contract(const float* L, const float* R, int64_t k_floats, int64_t ld
   int dev = 0, sms = 0;
   KPM_CUDA_TRY(cudaGetDevice(&dev));
   KPM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int KS = contract_splits(k_floats, sms);
+  const int KS = contract_splits(k_floats, sms, mu_tiles(Nm));
   float* part = nullptr;
   int* err = nullptr;
-  KPM_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&part), (size_t)KS * 256 * 512 * sizeof(float), s));
+  KPM_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&part), contract_part_floats(KS, mu_tiles(Nm)) * sizeof(float), s));
   KPM_CUDA_TRY(cudaMallocAsync(reinterpret_cast<void**>(&err), sizeof(int), s));
   KPM_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
   int rc = mu_contract(L, R, k_floats, ld, Nm, scale, accumulate, reinterpret_cast<double2*>(mu), part, KS, err, s);
@@ -283,60 +382,70 @@ int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double*
   KPM_TRY(ensure_f32_values(h, s));
   KPM_TRY(ensure_f32_values(v_op, s));
   Workspace& ws = h->ws;
-  const int64_t lda = 2 * h->n_pad;                        // floats per stored vector
-  const size_t mat = (size_t)256 * lda * sizeof(float);    // 256 rows, unused rows zero
-  const size_t vb = (size_t)h->n_pad * sizeof(float2);
-  KPM_TRY(ensure(ws.ckpt, 2 * mat));                        // A = L rows, B = R rows
+  // up to kMuGroup vectors advance together; a stored row is one packed [n_pad][Rg] complex64 vector set
+  const int G = pow2_group(std::min(R, kMuGroup));
+  const int64_t lda = 2 * (int64_t)G * h->n_pad;            // floats per stored row
+  const size_t mat = (size_t)256 * lda * sizeof(float);     // 256 rows; rows >= Nm stay zero
+  const size_t vb = (size_t)h->n_pad * G * sizeof(float2);
+  KPM_TRY(ensure(ws.ckpt, 2 * mat));                         // A = L rows, B = R rows
   KPM_TRY(ensure(ws.ta, vb));
   KPM_TRY(ensure(ws.tb, vb));
-  const int KS = contract_splits(lda, h->sm_count);
-  KPM_TRY(ensure(ws.part, (size_t)KS * 256 * 512 * sizeof(float)));
+  const int KS = contract_splits(lda, h->sm_count, mu_tiles(Nm));
+  KPM_TRY(ensure(ws.part, contract_part_floats(KS, mu_tiles(Nm)) * sizeof(float)));
   float* A = static_cast<float*>(ws.ckpt.p);
   float* B = A + (size_t)256 * lda;
-  if (Nm < 256) KPM_CUDA_TRY(cudaMemsetAsync(ws.ckpt.p, 0, 2 * mat, s));
-  const int grid_h = grid_for(h, 1, 1);
-  const int grid_v = grid_for(v_op, 1, 1);
-  for (int r = 0; r < R; ++r) {
-    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r, 1, true, ws.ta.p, s));
+  if (Nm < 256) {
+    const size_t tail = (size_t)(256 - Nm) * lda * sizeof(float);
+    KPM_CUDA_TRY(cudaMemsetAsync(A + (size_t)Nm * lda, 0, tail, s));
+    KPM_CUDA_TRY(cudaMemsetAsync(B + (size_t)Nm * lda, 0, tail, s));
+  }
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = std::min(G, pow2_group(R - r0));
+    const int64_t k = 2 * (int64_t)Rg * h->n_pad;  // floats of a row this group fills
+    const int grid_h = grid_for(h, Rg, vpt_for(true, Rg));
+    const int grid_v = grid_for(v_op, Rg, vpt_for(true, Rg));
+    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, true, ws.ta.p, s));
     // A[0] = V v, A[1] = H A[0], A[m+1] = 2 H A[m] - A[m-1]  (out of place, every row kept)
     StepParams pv = base_params(v_op, true);
     pv.tcur = ws.ta.p;
     pv.tout = A;
     pv.a_half = make_double2(0.5, 0.0);
-    KPM_TRY(launch_step(true, v_op->is_real, 1, MODE_APPLY, EPI_STORE, pv, grid_v, s));
+    KPM_TRY(launch_step(true, v_op->is_real, Rg, MODE_APPLY, EPI_STORE, pv, grid_v, s));
     StepParams ph = base_params(h, true);
     ph.tcur = A;
     ph.tout = A + lda;
-    KPM_TRY(launch_step(true, h->is_real, 1, MODE_FIRST, EPI_STORE, ph, grid_h, s));
+    KPM_TRY(launch_step(true, h->is_real, Rg, MODE_FIRST, EPI_STORE, ph, grid_h, s));
     for (int m = 1; m + 1 < Nm; ++m) {
       ph.tcur = A + (size_t)m * lda;
       ph.tprev = A + (size_t)(m - 1) * lda;
       ph.tout = A + (size_t)(m + 1) * lda;
-      KPM_TRY(launch_step(true, h->is_real, 1, MODE_NEXT, EPI_STORE, ph, grid_h, s));
+      KPM_TRY(launch_step(true, h->is_real, Rg, MODE_NEXT, EPI_STORE, ph, grid_h, s));
     }
     // T recursion on v (in place), B[m] = V T_m
     void* t_prev = ws.ta.p;  // T_0
     void* t_cur = ws.tb.p;
     pv.tcur = t_prev;
     pv.tout = B;
-    KPM_TRY(launch_step(true, v_op->is_real, 1, MODE_APPLY, EPI_STORE, pv, grid_v, s));
+    KPM_TRY(launch_step(true, v_op->is_real, Rg, MODE_APPLY, EPI_STORE, pv, grid_v, s));
     StepParams pt = base_params(h, true);
     pt.tcur = t_prev;
     pt.tout = t_cur;
-    KPM_TRY(launch_step(true, h->is_real, 1, MODE_FIRST, EPI_STORE, pt, grid_h, s));
+    KPM_TRY(launch_step(true, h->is_real, Rg, MODE_FIRST, EPI_STORE, pt, grid_h, s));
     for (int m = 1; m < Nm; ++m) {
       pv.tcur = t_cur;
       pv.tout = B + (size_t)m * lda;
-      KPM_TRY(launch_step(true, v_op->is_real, 1, MODE_APPLY, EPI_STORE, pv, grid_v, s));
+      KPM_TRY(launch_step(true, v_op->is_real, Rg, MODE_APPLY, EPI_STORE, pv, grid_v, s));
       if (m + 1 < Nm) {
         pt.tcur = t_cur;
         pt.tout = t_prev;
-        KPM_TRY(launch_step(true, h->is_real, 1, MODE_NEXT, EPI_STORE, pt, grid_h, s));
+        KPM_TRY(launch_step(true, h->is_real, Rg, MODE_NEXT, EPI_STORE, pt, grid_h, s));
         std::swap(t_prev, t_cur);
       }
     }
-    KPM_TRY(mu_contract(A, B, lda, lda, Nm, 1.0 / R, r > 0, reinterpret_cast<double2*>(mu),
+    // the group's rows contract over its k floats: sum over sites and the group's vectors
+    KPM_TRY(mu_contract(A, B, k, lda, Nm, 1.0 / R, r0 > 0, reinterpret_cast<double2*>(mu),
                         static_cast<float*>(ws.part.p), KS, h->err_flag, s));
+    r0 += Rg;
   }
   return KPM_OK;
 }

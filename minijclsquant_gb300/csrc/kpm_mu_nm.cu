@@ -404,6 +404,16 @@ int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double*
     const int64_t k = 2 * (int64_t)Rg * h->n_pad;  // floats of a row this group fills
     const int grid_h = grid_for(h, Rg, vpt_for(true, Rg));
     const int grid_v = grid_for(v_op, Rg, vpt_for(true, Rg));
+    // recursion steps: the staged producer-warp kernel (no moments), else the grid-stride kernel
+    const int occ = ws_ctas_f32(h->is_real, Rg, 1, h->L, 2);
+    const int64_t ntiles = h->n_pad / staged_tile_rows(true, Rg, 1);
+    const int grid_ws = occ > 0 ? (int)std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count) : 0;
+    auto next = [&](StepParams q) -> int {
+      q.vl = nullptr;
+      q.per_tile = 0;
+      return grid_ws > 0 ? launch_ws_f32(h->is_real, Rg, 1, q, grid_ws, s)
+                         : launch_step(true, h->is_real, Rg, MODE_NEXT, EPI_STORE, q, grid_h, s);
+    };
     KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, true, ws.ta.p, s));
     // A[0] = V v, A[1] = H A[0], A[m+1] = 2 H A[m] - A[m-1]  (out of place, every row kept)
     StepParams pv = base_params(v_op, true);
@@ -419,7 +429,7 @@ int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double*
       ph.tcur = A + (size_t)m * lda;
       ph.tprev = A + (size_t)(m - 1) * lda;
       ph.tout = A + (size_t)(m + 1) * lda;
-      KPM_TRY(launch_step(true, h->is_real, Rg, MODE_NEXT, EPI_STORE, ph, grid_h, s));
+      KPM_TRY(next(ph));
     }
     // T recursion on v (in place), B[m] = V T_m
     void* t_prev = ws.ta.p;  // T_0
@@ -438,7 +448,7 @@ int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double*
       if (m + 1 < Nm) {
         pt.tcur = t_cur;
         pt.tout = t_prev;
-        KPM_TRY(launch_step(true, h->is_real, Rg, MODE_NEXT, EPI_STORE, pt, grid_h, s));
+        KPM_TRY(next(pt));
         std::swap(t_prev, t_cur);
       }
     }

@@ -66,7 +66,7 @@ static __device__ __noinline__ void issue_tile(const TileCopy& tc, unsigned char
              bar, pol);
   const int64_t voff = row0 * vec_bytes_per_row;
   bulk_g2s(stage + tc.col_b + tc.val_b, tc.old + voff, tc.vec_slab, bar, pol);
-  bulk_g2s(stage + tc.col_b + tc.val_b + tc.vec_slab, tc.vl + voff, tc.vec_slab, bar, pol);
+  if (tc.vl) bulk_g2s(stage + tc.col_b + tc.val_b + tc.vec_slab, tc.vl + voff, tc.vec_slab, bar, pol);
 }
 
 template <typename T, bool REAL, int TPR, int VPT, int U>

@@ -13,7 +13,9 @@
 //
 // Moment partials follow the staged kernel: per CTA (strided tiles) or, for
 // batched operators (per_tile), flushed per (CTA, instance) run with a block
-// reduction over the compute warps alone (named barrier 1).
+// reduction over the compute warps alone (named barrier 1).  With p.vl null the
+// step stores T_{m+1} only (no left vector is copied, no moments), and with
+// p.tprev set T_{m-1} is read from there (out of place) instead of from tout.
 //
 // Every wait is bounded.  A compute warp whose wait runs out records
 // KPM_ERR_TIMEOUT and stops computing but still takes part in the named
@@ -76,7 +78,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
       const uint64_t pol = l2_evict_first_policy();
       tc.col = p.col;
       tc.val = static_cast<const unsigned char*>(p.val);
-      tc.old = static_cast<const unsigned char*>(p.tout);
+      tc.old = static_cast<const unsigned char*>(p.tprev ? p.tprev : p.tout);
       tc.vl = static_cast<const unsigned char*>(p.vl);
       tc.vl2 = nullptr;
       tc.ld = p.ld;
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
       tc.vec_slab = vec_b;
       tc.col_b = col_b;
       tc.val_b = val_b;
-      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + 2 * vec_b;
+      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + (p.vl ? 2 : 1) * vec_b;
       int issued = 0;
       for (int k = 0; k < my_count; ++k) {
         const int st = k % kWsStages;
@@ -107,6 +109,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
 
   int seg = p.per_tile ? p.seg_base[blockIdx.x] : 0;
   int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
+  const bool mom = p.vl != nullptr;
 
   const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
   Raw* tout = static_cast<Raw*>(p.tout);
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         acc[u] = finish(accum[u]);
-        unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
+        if (mom) unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
       }
       // the stage is no longer read: hand it back to the producer
       __syncwarp();
@@ -181,6 +184,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         tout[(row0 + u * RPB + rl) * TPR + sub] = pack(acc[u]);
+        if (!mom) continue;
 #pragma unroll
         for (int q = 0; q < VPT; ++q) {
           if (F32)
@@ -199,7 +203,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
         }
       }
     }
-    if (p.per_tile) {
+    if (p.per_tile && mom) {
       const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
       if (next_inst != cur_inst) {
         if (F32) {
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
     }
   }
 
-  if (!p.per_tile) {
+  if (!p.per_tile && mom) {
     if (F32) {
 #pragma unroll
       for (int q = 0; q < VPT; ++q) {

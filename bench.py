@@ -63,6 +63,7 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the differentiable-DOS measurement")
     ap.add_argument("--adj-cells", type=int, default=512)
     ap.add_argument("--adj-M", type=int, default=1024)
+    ap.add_argument("--adj-fd", type=int, default=64, help="parameters checked by central differences")
     ap.add_argument("--no-kubo", action="store_true", help="skip the Kubo-Greenwood mu_nm measurement")
     ap.add_argument("--kubo-cells", type=int, default=1024)
     ap.add_argument("--kubo-Nm", type=int, default=256)
@@ -419,8 +420,9 @@ def run_adjoint(a, steps, warmup):
     t_fb = timeit(fwd_bwd, steps)
     go, gh = onsite.grad.detach().cpu().numpy(), hop.grad.detach().cpu().numpy()
     pick = np.random.default_rng(7)
-    params = [("onsite", int(i)) for i in pick.choice(n, 32, replace=False)] + \
-             [("hopping", int(i)) for i in pick.choice(plan.n_bonds, 32, replace=False)]
+    half = a.adj_fd // 2
+    params = [("onsite", int(i)) for i in pick.choice(n, half, replace=False)] + \
+             [("hopping", int(i)) for i in pick.choice(plan.n_bonds, a.adj_fd - half, replace=False)]
     h = 1e-6
     worst = 0.0
     scale = max(np.max(np.abs(go)), np.max(np.abs(gh)))

@@ -39,19 +39,34 @@ struct AdjParams {
   double* grad;          // dL/dH per slot, [L][ld], accumulated
   double c;              // c_m
   double w;              // 1 for m = 1, else 2
+  // optional forward step of the segment recomputed next, out of place:
+  // rout = 2H rcur - rprev ([n_pad][R]); skipped when rout is null
+  const double2* rcur;
+  const double2* rprev;
+  double2* rout;
 };
 
-template <int R>
+// One adjoint order for every row, and (RC) one forward recompute step of the
+// next segment in the same pass over the operator: the two are independent, so
+// each row's entries are read once and the FP64 pipe gets two FMA streams.  The
+// recompute keeps the forward kernel's order (first product folded with
+// -t_{j-2}, then the slots in order), so it reproduces the forward pass exactly.
+template <int R, bool RC>
 __global__ void __launch_bounds__(kBlock) adj_step_kernel(const AdjParams p) {
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < p.n_pad;
        row += (int64_t)gridDim.x * blockDim.x) {
-    double ar[R], ai[R];
+    double ar[R], ai[R], fr[R], fi[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) {
       const double2 o = p.lam2[row * R + r];
       const double2 v = __ldg(p.u + row * R + r);
       ar[r] = fma(p.c, v.x, -o.x);   // c * conj(v) - lambda_{m+2}
       ai[r] = fma(-p.c, v.y, -o.y);
+      if (RC) {
+        const double2 q = p.rprev[row * R + r];
+        fr[r] = -q.x;
+        fi[r] = -q.y;
+      }
     }
     for (int s = 0; s < p.L; ++s) {
       const int j = __ldcs(p.col + (int64_t)s * p.ld + row);
@@ -61,10 +76,18 @@ __global__ void __launch_bounds__(kBlock) adj_step_kernel(const AdjParams p) {
         const double2 x = __ldg(p.lam1 + (int64_t)j * R + r);
         ar[r] = fma(h, x.x, ar[r]);
         ai[r] = fma(h, x.y, ai[r]);
+        if (RC) {
+          const double2 y = __ldg(p.rcur + (int64_t)j * R + r);
+          fr[r] = fma(h, y.x, fr[r]);
+          fi[r] = fma(h, y.y, fi[r]);
+        }
       }
     }
 #pragma unroll
-    for (int r = 0; r < R; ++r) p.lam2[row * R + r] = make_double2(ar[r], ai[r]);
+    for (int r = 0; r < R; ++r) {
+      p.lam2[row * R + r] = make_double2(ar[r], ai[r]);
+      if (RC) p.rout[row * R + r] = make_double2(fr[r], fi[r]);
+    }
     for (int s = 0; s < p.L; ++s) {
       const int j = __ldcs(p.col + (int64_t)s * p.ld + row);
       double g = 0.0;
@@ -82,7 +105,10 @@ __global__ void __launch_bounds__(kBlock) adj_step_kernel(const AdjParams p) {
 
 template <int R>
 static int launch_adj_r(const AdjParams& p, int grid, cudaStream_t s) {
-  adj_step_kernel<R><<<grid, kBlock, 0, s>>>(p);
+  if (p.rout)
+    adj_step_kernel<R, true><<<grid, kBlock, 0, s>>>(p);
+  else
+    adj_step_kernel<R, false><<<grid, kBlock, 0, s>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -233,7 +259,7 @@ int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream
   Workspace& ws = h->ws;
   const size_t vb = (size_t)h->n_pad * R * sizeof(double2);
   const int nseg = (M - 1 + ckpt - 1) / ckpt;
-  KPM_TRY(ensure(ws.seg, (size_t)ckpt * vb));
+  KPM_TRY(ensure(ws.seg, (size_t)2 * ckpt * vb));  // two segment buffers: consumed, recomputed
   KPM_TRY(ensure(ws.acc, vb));
   KPM_TRY(ensure(ws.acc2, vb));
   KPM_TRY(ensure(ws.grad, (size_t)h->L * h->n_pad * sizeof(double)));
@@ -246,21 +272,36 @@ int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream
   KPM_CUDA_TRY(cudaMemsetAsync(lb, 0, vb, s));
   KPM_CUDA_TRY(cudaMemsetAsync(ws.grad.p, 0, (size_t)h->L * h->n_pad * sizeof(double), s));
   char* ck = static_cast<char*>(ws.ckpt.p);
-  char* seg = static_cast<char*>(ws.seg.p);
+  char* segs[2] = {static_cast<char*>(ws.seg.p), static_cast<char*>(ws.seg.p) + (size_t)ckpt * vb};
   const int grid = grid_rows(h);
   StepParams p = base_params(h, false);
+  // segment q holds t_{k0} .. t_{k0 + count - 1}, k0 = q * ckpt; the adjoint orders
+  // m = k0 + count .. k0 + 1 use t_{m-1}
+  auto seg_count = [&](int q) { return std::min(q * ckpt + ckpt, M - 1) - q * ckpt; };
+  auto load_ckpt = [&](int q, char* dst) -> int {
+    KPM_CUDA_TRY(cudaMemcpyAsync(dst, ck + (size_t)q * 2 * vb, (seg_count(q) > 1 ? 2 : 1) * vb,
+                                 cudaMemcpyDeviceToDevice, s));
+    return KPM_OK;
+  };
+  auto recompute_step = [&](char* sg, int j) -> int {  // t_j of a segment from t_{j-1}, t_{j-2}
+    p.tcur = sg + (size_t)(j - 1) * vb;
+    p.tprev = sg + (size_t)(j - 2) * vb;
+    p.tout = sg + (size_t)j * vb;
+    return launch_step(false, true, R, MODE_NEXT, EPI_STORE, p, grid, s);
+  };
+  // the last segment is recomputed alone; every earlier one during the adjoint
+  // orders of the segment after it
+  int cur = 0;
+  KPM_TRY(load_ckpt(nseg - 1, segs[cur]));
+  for (int j = 2; j < seg_count(nseg - 1); ++j) KPM_TRY(recompute_step(segs[cur], j));
   for (int q = nseg - 1; q >= 0; --q) {
     const int k0 = q * ckpt;
-    const int m_hi = std::min(k0 + ckpt, M - 1);
-    const int count = m_hi - k0;  // t_{k0} .. t_{m_hi - 1}
-    KPM_CUDA_TRY(cudaMemcpyAsync(seg, ck + (size_t)q * 2 * vb, (count > 1 ? 2 : 1) * vb, cudaMemcpyDeviceToDevice, s));
-    for (int j = 2; j < count; ++j) {  // recompute the segment out of place
-      p.tcur = seg + (size_t)(j - 1) * vb;
-      p.tprev = seg + (size_t)(j - 2) * vb;
-      p.tout = seg + (size_t)j * vb;
-      KPM_TRY(launch_step(false, true, R, MODE_NEXT, EPI_STORE, p, grid, s));
-    }
-    for (int m = m_hi; m >= k0 + 1; --m) {
+    const int count = seg_count(q);
+    const int nxt = cur ^ 1;
+    const int rc_steps = q > 0 ? std::max(0, seg_count(q - 1) - 2) : 0;
+    if (q > 0) KPM_TRY(load_ckpt(q - 1, segs[nxt]));
+    int i = 0;
+    for (int m = k0 + count; m >= k0 + 1; --m) {
       AdjParams a;
       a.val = static_cast<const double*>(h->val64);
       a.col = h->col;
@@ -270,13 +311,23 @@ int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream
       a.lam1 = la;
       a.lam2 = lb;
       a.u = static_cast<const double2*>(ws.vl.p);
-      a.tprev = reinterpret_cast<const double2*>(seg + (size_t)(m - 1 - k0) * vb);
+      a.tprev = reinterpret_cast<const double2*>(segs[cur] + (size_t)(m - 1 - k0) * vb);
       a.grad = static_cast<double*>(ws.grad.p);
       a.c = ch[m];
       a.w = m == 1 ? 1.0 : 2.0;
+      a.rcur = a.rprev = nullptr;
+      a.rout = nullptr;
+      if (i < rc_steps) {  // fused: t_{i+2} of segment q - 1
+        a.rprev = reinterpret_cast<const double2*>(segs[nxt] + (size_t)i * vb);
+        a.rcur = reinterpret_cast<const double2*>(segs[nxt] + (size_t)(i + 1) * vb);
+        a.rout = reinterpret_cast<double2*>(segs[nxt] + (size_t)(i + 2) * vb);
+        ++i;
+      }
       KPM_TRY(launch_adj(R, a, grid, s));
       std::swap(la, lb);  // lambda_m becomes lambda_{m'+1} of the next (lower) order
     }
+    for (; i < rc_steps; ++i) KPM_TRY(recompute_step(segs[nxt], i + 2));
+    cur = nxt;
   }
   const int64_t total = h->n * (int64_t)h->L;
   slots_to_rows_kernel<<<(int)std::min<int64_t>((total + 255) / 256, 65536), 256, 0, s>>>(

@@ -69,7 +69,7 @@ def test_batched_kernel_variants_agree(cuda_lib, monkeypatch, kernel, dtype, R):
     v = batched.ensemble_vectors(B.rows, R)
     mu = B.moments(90, v, dtype=dtype)
     cfg = B.step_config(dtype, R)
-    assert (cfg["kind"], cfg["rows_per_thread"]) == KINDS[kernel] or cfg["kind"] == 0, cfg
+    assert (cfg["kind"], cfg["rows_per_thread"]) == KINDS[kernel], cfg
     for k in range(6):
         o, n = int(B.offsets[k]), int(B.rows[k])
         for r in range(R):

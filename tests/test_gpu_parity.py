@@ -241,7 +241,7 @@ def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R):
     code = _capi.KPM_C128 if dtype == "c128" else _capi.KPM_C64
     assert cuda_lib.kpm_ell_step_config(op.handle, code, R, ctypes.byref(kind), ctypes.byref(U), None, None) == 0
     assert (kind.value, U.value) == {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2), "ws1": (2, 1),
-                                     "ws2": (2, 2)}[kernel] or kind.value == 0
+                                     "ws2": (2, 2)}[kernel]
     assert cuda_lib.kpm_ell_check(op.handle, None) == 0
     for r in range(R):
         ref = oracle.rec_A_tab(150, Hk.data, Hk.indices, Hk.len_row, vs[r])

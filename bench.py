@@ -283,14 +283,22 @@ def run_reference_arm(a):
     print(json.dumps(line), flush=True)
 
 
-def launches_per_recursion(M, R):
+def executed_steps(M, doubled):
+    """Recursion steps after the first one: M - 2 (direct) or ceil(M/2) - 1 (doubled)."""
+    return (M + 1) // 2 - 1 if doubled else max(0, M - 2)
+
+
+def launches_per_recursion(M, R, doubled=False):
     groups = []
     r = R
     while r > 0:
         g = 8 if r >= 8 else 4 if r >= 4 else 2 if r >= 2 else 1
         groups.append(g)
         r -= g
-    per_group = 2 + 1 + max(0, M - 2) + ((M - 1) // 128 if M > 128 else 0) + 1
+    steps = executed_steps(M, doubled)
+    # packing (2), first step, the steps, their chunked reductions; doubled: half
+    # norms, the first-step reduction and the assembly of the moments
+    per_group = 2 + 1 + steps + (steps + 1 + 127) // 128 + (3 if doubled else 0)
     return per_group * len(groups)
 
 
@@ -340,21 +348,34 @@ def run_batched(a, hbm_peak, steps, warmup):
         torch.cuda.synchronize()
         return mu, e0.elapsed_time(e1) / k_steps
 
+    doubled = bool(B.doubling)  # the direct recursion unless doubling was requested
     mu64, ms64 = timed("c64", steps, warmup)
     mu128, ms128 = timed("c128", 1, 1)
     cfg64, cfg128 = B.step_config("c64", R), B.step_config("c128", R)
+    # the opt-in doubled moments of the same ensemble, both precisions
+    B.set_doubling(True)
+    mu64x, ms64x = timed("c64", 1, 1)
+    mu128x, ms128x = timed("c128", 1, 1)
+    B.set_doubling(doubled)
     mu64 = mu64.cpu().numpy()
-    mu128 = mu128.cpu().numpy()
-    site_steps = float(B.n_total) * R * (M - 1)
+    mu128d = mu128.cpu().numpy()  # errors are taken against direct complex128, the reference's algorithm
+    mu64x = mu64x.cpu().numpy()
+    d64x = batched.batched_dos(mu64x, bnds, M)
+    site_steps = float(B.n_total) * R * (M - 1)  # per moment delivered
     val64 = site_steps / (ms64 * 1e-3)
     val128 = site_steps / (ms128 * 1e-3)
     d64 = batched.batched_dos(mu64, bnds, M)
-    d128 = batched.batched_dos(mu128, bnds, M)
+    d128 = batched.batched_dos(mu128d, bnds, M)
     dos_err = max(float(np.max(np.abs(x[:, 1] - y[:, 1])) / np.max(np.abs(y[:, 1]))) for x, y in zip(d64, d128))
-    mom_err = np.abs(mu64 - mu128) / np.abs(mu128[:, :, :1])
+    dos_err_x = max(float(np.max(np.abs(x[:, 1] - y[:, 1])) / np.max(np.abs(y[:, 1]))) for x, y in zip(d64x, d128))
+    mom_err = np.abs(mu64 - mu128d) / np.abs(mu128d[:, :, :1])
     per_order = mom_err.max(axis=(0, 1))
-    bytes_per_site_step = L * (8 + 4) / R + 4 * 8  # split-float value (8 B) + index per slot
-    ach = bytes_per_site_step * val64 / 1e9
+    # bytes per executed site-step: split-float value (8 B) + index per slot, T_m, T_{m-1},
+    # T_{m+1}, and v_l (direct) or |v|^2/2 (doubled)
+    bytes_per_site_step = L * (8 + 4) / R + 3 * 8 + (4 if doubled else 8)
+    exec_steps = executed_steps(M, doubled) + 1
+    exec_rate = float(B.n_total) * R * exec_steps / (ms64 * 1e-3)
+    ach = bytes_per_site_step * exec_rate / 1e9
     return {"workload": "%d honeycomb instances, sides U{32..%d} cells (%d sites total), W~U[0,2] eV, R=%d, M=%d"
                         % (B.n_inst, a.batch_side_max, B.n_total, R, M),
             "value": val64, "unit": UNIT, "ms_per_step": ms64, "dtype": "c64 recursion, f64 moment accumulation",
@@ -362,12 +383,17 @@ def run_batched(a, hbm_peak, steps, warmup):
                                          "frac": ach / hbm_peak, "bytes_per_site_step": bytes_per_site_step},
             "c128_same_ensemble": {"value": val128, "ms_per_step": ms128},
             "speedup_c64_vs_c128": val64 / val128,
+            "doubling": {"used_above": doubled,
+                         "note": "opt-in; ceil(M/2)-1 steps; values count site-steps per moment delivered",
+                         "c64": {"value": site_steps / (ms64x * 1e-3), "ms_per_step": ms64x,
+                                 "dos_error_max_over_instances": dos_err_x},
+                         "c128": {"value": site_steps / (ms128x * 1e-3), "ms_per_step": ms128x}},
             "dos_error_max_over_instances": dos_err,
             "moment_error_vs_c128": {"max_rel_mu0": float(per_order.max()),
                                      "by_order": {str(m): float(per_order[m]) for m in (1, 10, 100, 500, M - 1) if m < M}},
             "setup_s": setup_s, "graph": "one CUDA graph launch per recursion",
             "step_kernel": {"c64": cfg64, "c128": cfg128},
-            "gpu_launches_per_step": 2 + 1 + max(0, M - 2) + 1}
+            "gpu_launches_per_step": 1 + executed_steps(M, doubled) + (M + 127) // 128 + (3 if doubled else 0)}
 
 
 def run_adjoint(a, steps, warmup):
@@ -604,6 +630,7 @@ def run_ours(a):
     ms_max = max_over_ranks(ms, world)
     site_steps = float(n) * R * (M - 1) * a.steps
     value = site_steps * world / (ms_max * 1e-3)
+    doubled = bool(op.doubling)
 
     # sanity: mu_0 = N for unit-modulus vectors
     mu_h = mu.cpu().numpy()
@@ -613,7 +640,8 @@ def run_ours(a):
     s_v = 16 if a.dtype == "c128" else 8
     # complex128: FP64 values; complex64: exact float pairs (hi, lo) -- 8 B real, 16 B complex either way
     val_bytes = 8 if op.is_real else 16
-    bytes_per_row = L * (val_bytes + 4) + R * 4 * s_v
+    # per executed step: T_m gathered once, T_{m-1}, T_{m+1}, and v_l (direct) or |v|^2/2 (doubled)
+    bytes_per_row = L * (val_bytes + 4) + R * (3 * s_v + (s_v // 4 if doubled else s_v))
     bytes_per_launch = float(n) * bytes_per_row
     avg_launch_s = (loop_ms.value * 1e-3) / max(1, launches.value)
     achieved_gbs = bytes_per_launch / avg_launch_s / 1e9
@@ -639,7 +667,7 @@ def run_ours(a):
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
     fma_rate = ctypes.c_double()
     _capi.check(lib.kpm_measure_fp64_fma_rate(ctypes.byref(fma_rate), ctypes.c_void_p(int(stream.cuda_stream))))
-    fma_per_site_step = (2 * L if op.is_real else 4 * L) + 4
+    fma_per_site_step = (2 * L if op.is_real else 4 * L) + (6 if doubled else 4)
     fp64 = None
     if a.dtype == "c128":
         ach = fma_per_site_step * float(n) * R / avg_launch_s
@@ -652,8 +680,32 @@ def run_ours(a):
             "config": {"workload": workload_desc(a, n), "sites": n, "M": M, "R": R, "len_row": L, "W": a.W,
                        "bounds": "Gershgorin x 1.01", "l2": "inputs larger than L2 (vector set %.2f GB)"
                        % (n * R * s_v / 1e9), "parallelism": "replicas x%d" % world},
-            "roofline": roofline, "fp64": fp64, "gpu_launches": launches_per_recursion(M, R) * a.steps,
+            "roofline": roofline, "fp64": fp64, "gpu_launches": launches_per_recursion(M, R, doubled) * a.steps,
             "hbm_gbs": achieved_gbs}
+    # the opt-in doubled moments on the same handle (H is Hermitian): the same M moments
+    # from ceil(M/2) - 1 recursion steps; value counts site-steps per moment delivered
+    if op.hermitian and not doubled and a.dtype == "c128":
+        op.set_doubling(True)
+        step()
+        torch.cuda.synchronize()
+        d0 = torch.cuda.Event(enable_timing=True)
+        d1 = torch.cuda.Event(enable_timing=True)
+        d0.record(stream)
+        for _ in range(a.steps):
+            mu_dbl = step()
+        d1.record(stream)
+        torch.cuda.synchronize()
+        op.set_doubling(False)
+        ms_d = max_over_ranks(d0.elapsed_time(d1), world) / a.steps
+        dk = ctypes.c_int()
+        _capi.check(lib.kpm_ell_props(op.handle, None, ctypes.byref(dk)))
+        line["doubling"] = {
+            "value": float(n) * R * (M - 1) * world / (ms_d * 1e-3), "ms_per_step": ms_d,
+            "executed_steps_per_recursion": executed_steps(M, True) + 1, "moments_per_recursion": M,
+            "fma_per_executed_site_step": fma_per_site_step + 2,
+            "max_abs_diff_vs_direct_over_mu0": float(np.max(np.abs(mu_dbl.cpu().numpy() - mu_h))
+                                                     / np.max(np.abs(mu_h[:, 0]))),
+            "note": "opt-in (KPM_FLAG_DOUBLING); value counts site-steps per moment delivered, N R (M-1)"}
     clocks = clk.summary()
     if clocks is not None:
         line["clocks"] = clocks

@@ -52,7 +52,8 @@ extern "C" {
 
 /* ---- operator creation flags ------------------------------------------- */
 #define KPM_FLAG_DEVICE_PTRS 1u   /* data/indices are device pointers        */
-#define KPM_FLAG_SPLIT_DIAG 2u    /* store slots with col == row separately   */
+#define KPM_FLAG_SPLIT_DIAG 2u    /* accepted; the diagonal stays an ELL slot  */
+#define KPM_FLAG_DOUBLING 4u      /* DOS moments by the doubling identity      */
 
 typedef struct kpm_ell_s kpm_ell;
 
@@ -91,6 +92,19 @@ int kpm_ell_check(kpm_ell* h, void* stream);
  * thread per tile; CTAs; measured us per step. */
 int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                         float* step_us);
+/* Doubling (opt-in: KPM_FLAG_DOUBLING at creation or kpm_ell_set_doubling).
+ * kpm_ell_create checks on the device whether H == H^dagger exactly (entry by
+ * entry, duplicate slots summed).  For such an operator with doubling on, moment
+ * calls with v_l == NULL and mu_rr == NULL (DOS moments, M >= 4) use
+ *   mu_{2k} = 2 sum_i (|t_k,i|^2 - |v_i|^2/2),  mu_{2k+1} = 2 <t_{k+1}|t_k> - mu_1,
+ * t_k = T_k(H) v: ceil(M/2) - 1 recursion steps instead of M - 2.  complex128
+ * results agree with the direct recursion to ~1e-16 mu_0.  In complex64 every
+ * step's FP32 rounding enters all later doubled moments alike (an error coherent
+ * across orders, ~1e-8 mu_0), so complex64 DOS work should stay direct.  The
+ * reference always runs the M - 2 steps (jclsquant/recurrence_functions.py:18-38).
+ * kpm_ell_props reports whether H is Hermitian and whether DOS calls double. */
+int kpm_ell_props(const kpm_ell* h, int* hermitian, int* doubling);
+int kpm_ell_set_doubling(kpm_ell* h, int on);
 
 /*
  * y <- b*y + a*H x on R vectors ([R][n] c128, device).
@@ -209,6 +223,10 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
  * No counterpart in the reference. */
 int kpm_batch_step_config(kpm_batch* b, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                           float* step_us, void* stream);
+/* Doubling for batched operators, as kpm_ell_props / kpm_ell_set_doubling: the
+ * stacked operator is Hermitian when every instance is. */
+int kpm_batch_props(const kpm_batch* b, int* hermitian, int* doubling);
+int kpm_batch_set_doubling(kpm_batch* b, int on);
 int kpm_batch_check(kpm_batch* b, void* stream);
 
 /* ---- moments without any device allocation --------------------------------

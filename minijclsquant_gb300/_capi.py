@@ -28,6 +28,7 @@ KPM_C64 = 1
 
 KPM_FLAG_DEVICE_PTRS = 1
 KPM_FLAG_SPLIT_DIAG = 2
+KPM_FLAG_DOUBLING = 4
 
 DTYPES = {"c128": KPM_C128, "complex128": KPM_C128, "c64": KPM_C64, "complex64": KPM_C64}
 
@@ -66,6 +67,10 @@ SIGNATURES = {
     "kpm_batch_destroy": (_I, [_P]),
     "kpm_batch_info": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I64), ctypes.POINTER(_I64), ctypes.POINTER(_I)]),
     "kpm_batch_moments": (_I, [_P, _I, _I, _I, _P, _P, _P]),
+    "kpm_ell_props": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "kpm_ell_set_doubling": (_I, [_P, _I]),
+    "kpm_batch_props": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
+    "kpm_batch_set_doubling": (_I, [_P, _I]),
     "kpm_batch_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                    ctypes.POINTER(ctypes.c_float), _P]),
     "kpm_batch_check": (_I, [_P, _P]),

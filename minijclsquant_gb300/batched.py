@@ -72,6 +72,23 @@ class BatchedELL:
 
     _KINDS = {0: "grid-stride", 1: "staged", 2: "staged+producer-warp"}
 
+    @property
+    def hermitian(self) -> bool:
+        """Every instance is Hermitian (checked on the device at creation)."""
+        h = ctypes.c_int()
+        _capi.check(_capi.lib().kpm_batch_props(self._h, ctypes.byref(h), None), "kpm_batch_props")
+        return bool(h.value)
+
+    @property
+    def doubling(self) -> bool:
+        """Whether moments use the doubling identity (ceil(M/2) - 1 steps for M moments)."""
+        d = ctypes.c_int()
+        _capi.check(_capi.lib().kpm_batch_props(self._h, None, ctypes.byref(d)), "kpm_batch_props")
+        return bool(d.value)
+
+    def set_doubling(self, on: bool):
+        _capi.check(_capi.lib().kpm_batch_set_doubling(self._h, int(bool(on))), "kpm_batch_set_doubling")
+
     def step_config(self, dtype="c64", R=2, stream=None):
         """The recursion-step kernel the batched autotuner chose for (dtype, R):
         dict(kind, kernel, rows_per_thread, grid, step_us); tunes it first if needed."""

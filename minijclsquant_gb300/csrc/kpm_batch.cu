@@ -28,8 +28,8 @@ struct kpm_batch_s {
   kpm_ell_s* op = nullptr;             // the stacked operator
   // graph cache
   struct G {
-    int f32, R, M, kind;
-    const void* bufs[5];  // workspace pointers the graph was recorded with
+    int f32, R, M, kind, dbl;
+    const void* bufs[8];  // workspace pointers the graph was recorded with
     cudaGraphExec_t exec;
   };
   std::vector<G> graphs;
@@ -48,6 +48,7 @@ struct kpm_batch_s {
     int* d_seg_base = nullptr;         // staged: first slot of each CTA
     int chunk = 2;
     float step_us = 0.f;               // tuned time of one later step
+    int dbl = 0;                       // doubled DOS moments: two partial sets per step
   };
   std::vector<Plan> plans;
 };
@@ -128,14 +129,15 @@ __global__ void batch_pack_kernel(const double2* __restrict__ src, const int64_t
   }
 }
 
-// part[step][slot][R] -> mu[k][r][m0 + step]; instance k owns slots [ibeg[k], ibeg[k+1]).
-// One CTA per (r, instance, step); fixed-order strided sums and a fixed tree.
-__global__ void batch_reduce_kernel(const double2* __restrict__ part, int64_t nslots,
+// part[step * step_stride + slot * R + r] -> mu[k][r][m0 + step]; instance k owns
+// slots [ibeg[k], ibeg[k+1]).  One CTA per (r, instance, step); fixed-order
+// strided sums and a fixed tree.
+__global__ void batch_reduce_kernel(const double2* __restrict__ part, int64_t step_stride,
                                     const int64_t* __restrict__ ibeg, int R, double2* __restrict__ mu, int M,
                                     int m0) {
   const int r = blockIdx.x, k = blockIdx.y, step = blockIdx.z;
   const int64_t t0 = ibeg[k], t1 = ibeg[k + 1];
-  const double2* base = part + (int64_t)step * nslots * R;
+  const double2* base = part + (int64_t)step * step_stride;
   double sr = 0.0, si = 0.0;
   for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
     const double2 v = base[t * R + r];
@@ -157,13 +159,6 @@ __global__ void batch_reduce_kernel(const double2* __restrict__ part, int64_t ns
 }
 
 int grid1(int64_t total) { return (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 65536)); }
-
-int check_cuda(cudaError_t e) {
-  if (e == cudaSuccess) return KPM_OK;
-  set_last_cuda_error(e);
-  (void)cudaGetLastError();
-  return e == cudaErrorMemoryAllocation ? KPM_ERR_OOM : KPM_ERR_CUDA;
-}
 
 // Steps whose partials are buffered before a segmented reduction.
 int batch_chunk(int64_t nslots, int R) {
@@ -226,6 +221,7 @@ int plan_next(kpm_batch_s* b, bool f32, int R, const kpm_batch_s::Plan& pl, Step
   kpm_ell_s* h = b->op;
   p.tile_inst = pl.d_tile_inst;
   p.seg_base = pl.d_seg_base;
+  p.part_set_stride = pl.nslots * R;
   if (pl.kind == 1) {
     p.per_tile = 1;
     return f32 ? launch_staged_f32(h->is_real, R, pl.U, p, pl.grid, s) : launch_staged_f64(h->is_real, R, pl.U, p, pl.grid, s);
@@ -261,9 +257,9 @@ StepParams batch_params(kpm_ell_s* h, bool f32) {
 // Each candidate is timed on the stacked operator itself (a few launches on
 // zeroed vectors) and the fastest is kept.  KPM_STEP_KERNEL forces one
 // (simple|staged1|staged2|ws1|ws2).
-int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_s::Plan** out) {
+int batch_plan(kpm_batch_s* b, bool f32, int R, bool dbl, cudaStream_t s, const kpm_batch_s::Plan** out) {
   for (auto& pl : b->plans)
-    if (pl.f32 == (int)f32 && pl.R == R) {
+    if (pl.f32 == (int)f32 && pl.R == R && pl.dbl == (int)dbl) {
       *out = &pl;
       return KPM_OK;
     }
@@ -271,6 +267,7 @@ int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_
   kpm_batch_s::Plan base;
   base.f32 = (int)f32;
   base.R = R;
+  base.dbl = (int)dbl;
   base.tile_first = kBlock / (R / ((f32 && R >= 2) ? 2 : 1));
   base.ntiles_first = h->n_pad / base.tile_first;
   std::vector<int64_t> ib(b->n_inst + 1);
@@ -294,6 +291,7 @@ int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_
   int rc = KPM_OK;
   for (int kind = 1; kind <= 2 && rc == KPM_OK; ++kind)
     for (int U = 1; U <= 2 && rc == KPM_OK; ++U) {
+      if (dbl && kind == 1) continue;  // doubling: grid-stride and producer-warp kernels
       if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
       const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, R, U, h->L, 2) : staged_ctas_f64(h->is_real, R, U, h->L, 2))
                                 : (f32 ? ws_ctas_f32(h->is_real, R, U, h->L, 2) : ws_ctas_f64(h->is_real, R, U, h->L, 2));
@@ -322,14 +320,21 @@ int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_
     for (auto& c : cands) max_slots = std::max(max_slots, c.nslots);
     Workspace& ws = h->ws;
     const size_t vb = (size_t)h->n_pad * R * (f32 ? sizeof(float2) : sizeof(double2));
-    rc = ensure(ws.part, (size_t)max_slots * R * sizeof(double2));
+    rc = ensure(ws.part, (size_t)2 * max_slots * R * sizeof(double2));
+    if (rc == KPM_OK) rc = ensure(ws.vr, vb);
     if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.ta.p, 0, vb, s));
     if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.tb.p, 0, vb, s));
     if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.vl.p, 0, vb, s));
+    if (rc == KPM_OK) rc = check_cuda(cudaMemsetAsync(ws.vr.p, 0, vb, s));
     StepParams p = batch_params(h, f32);
     p.tcur = ws.ta.p;
     p.tout = ws.tb.p;
     p.part = static_cast<double2*>(ws.part.p);
+    if (dbl) {
+      p.vl = nullptr;
+      p.dbl = 1;
+      p.hv = ws.vr.p;
+    }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     if (rc == KPM_OK) rc = check_cuda(cudaEventCreate(&e0));
     if (rc == KPM_OK) rc = check_cuda(cudaEventCreate(&e1));
@@ -358,7 +363,7 @@ int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_
   }
   kpm_batch_s::Plan pl = cands[best];
   pl.step_us = us[best];
-  pl.chunk = batch_chunk(pl.nslots, R);
+  pl.chunk = batch_chunk((dbl ? 2 : 1) * pl.nslots, R);
   b->plans.push_back(pl);
   *out = &b->plans.back();
   return KPM_OK;
@@ -366,8 +371,10 @@ int batch_plan(kpm_batch_s* b, bool f32, int R, cudaStream_t s, const kpm_batch_
 
 // Partial-buffer elements (double2) a plan needs: two first-step blocks, then chunk NEXT blocks.
 int64_t plan_part_elems(const kpm_batch_s::Plan& pl, int R) {
-  return 2 * pl.ntiles_first * R + (int64_t)pl.chunk * pl.nslots * R;
+  return 2 * pl.ntiles_first * R + (int64_t)pl.chunk * (pl.dbl ? 2 : 1) * pl.nslots * R;
 }
+
+bool batch_doubling(const kpm_batch_s* b, int M) { return use_doubling(b->op, M); }
 
 // The launch sequence of one batched recursion on internal buffers:
 // ta = T_0 (packed), tb = T_1, vl = left vectors, part = partials, mu_int = [n_inst][R][M].
@@ -387,8 +394,44 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Pl
               : launch_step_f64(h->is_real, R, MODE_FIRST, EPI_STORE | EPI_MOM1, p, (int)pl.ntiles_first, s));
   {
     dim3 g(R, b->n_inst, M >= 2 ? 2 : 1);
-    batch_reduce_kernel<<<g, 128, 0, s>>>(part_first, pl.ntiles_first, pl.d_ibeg_first, R, mu, M, 0);
+    batch_reduce_kernel<<<g, 128, 0, s>>>(part_first, pl.ntiles_first * R, pl.d_ibeg_first, R, mu, M, 0);
     KPM_CUDA_TRY(cudaGetLastError());
+  }
+  if (pl.dbl) {
+    // doubled: steps m = 2 .. K = ceil(M/2), sets <t_m|t_{m-1}> and sum(|t_{m-1}|^2 - hv) per instance
+    const int K = (M + 1) / 2;
+    if (f32)  // mu_1 exactly for the float start vectors (enters every odd moment)
+      KPM_TRY(mu1_exact(h, ws.vl.p, R, b->d_poff, b->n_inst, mu, M, 0, ws.tc, s));
+    const int64_t sstride = 2 * pl.nslots * R;
+    double2* rb = static_cast<double2*>(ws.red.p);
+    double2* rd = rb + (size_t)b->n_inst * R * (K + 1);
+    const double* corr = reinterpret_cast<const double*>(rd + (size_t)b->n_inst * R * (K + 1));
+    p.vl = nullptr;
+    p.dbl = 1;
+    p.hv = ws.vr.p;
+    auto reduce = [&](int m0, int steps) -> int {
+      dim3 g(R, b->n_inst, steps);
+      batch_reduce_kernel<<<g, 128, 0, s>>>(part, sstride, pl.d_ibeg, R, rb, K + 1, m0);
+      batch_reduce_kernel<<<g, 128, 0, s>>>(part + pl.nslots * R, sstride, pl.d_ibeg, R, rd, K + 1, m0);
+      KPM_CUDA_TRY(cudaGetLastError());
+      return KPM_OK;
+    };
+    void* tprev = ws.ta.p;
+    void* tcur = ws.tb.p;
+    int m0 = 2;
+    for (int m = 2; m <= K; ++m) {
+      if (m - m0 == pl.chunk) {
+        KPM_TRY(reduce(m0, pl.chunk));
+        m0 = m;
+      }
+      p.tcur = tcur;
+      p.tout = tprev;
+      p.part = part + (int64_t)(m - m0) * sstride;
+      KPM_TRY(plan_next(b, f32, R, pl, p, s));
+      std::swap(tprev, tcur);
+    }
+    if (K + 1 > m0) KPM_TRY(reduce(m0, K + 1 - m0));
+    return assemble_doubled(rb, rd, corr, b->n_inst * R, K, M, mu, M, 0, s);
   }
   void* tprev = ws.ta.p;
   void* tcur = ws.tb.p;
@@ -396,7 +439,7 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Pl
   for (int m = 2; m < M; ++m) {
     if (m - m0 == pl.chunk) {
       dim3 g(R, b->n_inst, pl.chunk);
-      batch_reduce_kernel<<<g, 128, 0, s>>>(part, pl.nslots, pl.d_ibeg, R, mu, M, m0);
+      batch_reduce_kernel<<<g, 128, 0, s>>>(part, pl.nslots * R, pl.d_ibeg, R, mu, M, m0);
       KPM_CUDA_TRY(cudaGetLastError());
       m0 = m;
     }
@@ -408,7 +451,7 @@ int record_batched(kpm_batch_s* b, bool f32, int R, int M, const kpm_batch_s::Pl
   }
   if (M > m0) {
     dim3 g(R, b->n_inst, M - m0);
-    batch_reduce_kernel<<<g, 128, 0, s>>>(part, pl.nslots, pl.d_ibeg, R, mu, M, m0);
+    batch_reduce_kernel<<<g, 128, 0, s>>>(part, pl.nslots * R, pl.d_ibeg, R, mu, M, m0);
     KPM_CUDA_TRY(cudaGetLastError());
   }
   return KPM_OK;
@@ -502,6 +545,8 @@ int kpm_batch_create(kpm_batch** out, int n_inst, const int64_t* inst_rows, int 
   release(st_data);
   release(st_idx);
   release(flag);
+  h->doubling = 0;
+  if ((rc = check_hermitian(h, s)) != KPM_OK) return fail(rc);
   *out = b;
   return KPM_OK;
 }
@@ -547,7 +592,7 @@ int kpm_batch_step_config(kpm_batch* b, int dtype, int R, int* kind, int* rows_p
   KPM_TRY(ensure(h->ws.tb, vb));
   KPM_TRY(ensure(h->ws.vl, vb));
   const kpm_batch_s::Plan* plan = nullptr;
-  KPM_TRY(batch_plan(b, f32, R, s, &plan));
+  KPM_TRY(batch_plan(b, f32, R, batch_doubling(b, 4), s, &plan));
   if (kind) *kind = plan->kind;
   if (rows_per_thread) *rows_per_thread = plan->kind == 0 ? 1 : plan->U;
   if (grid) *grid = plan->grid;
@@ -569,22 +614,39 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
   KPM_TRY(ensure(ws.tb, vb));
   KPM_TRY(ensure(ws.vl, vb));
   KPM_TRY(ensure(b->mu_int, (size_t)b->n_inst * R * M * sizeof(double2)));
-  // kernel choice and partial-slot layout (built once per precision and R)
+  // kernel choice and partial-slot layout (built once per precision, R and mode)
+  const bool dbl = batch_doubling(b, M);
   const kpm_batch_s::Plan* plan = nullptr;
-  KPM_TRY(batch_plan(b, f32, R, s, &plan));
+  KPM_TRY(batch_plan(b, f32, R, dbl, s, &plan));
   KPM_TRY(ensure(ws.part, (size_t)plan_part_elems(*plan, R) * sizeof(double2)));
+  if (dbl) {
+    KPM_TRY(ensure(ws.vr, vb));
+    KPM_TRY(ensure(ws.red, (size_t)2 * b->n_inst * R * ((M + 1) / 2 + 1) * sizeof(double2) +
+                               (size_t)b->n_inst * R * sizeof(double)));
+    // scratch of the exact mu_1 (at most 64 partial blocks per instance and vector),
+    // sized here because nothing may allocate while the graph is being recorded
+    if (f32) KPM_TRY(ensure(ws.tc, (size_t)b->n_inst * 64 * R * sizeof(double2)));
+  }
   // inputs into the internal buffers (outside the graph)
   batch_pack_kernel<<<grid1(h->n_pad * R), 256, 0, s>>>(reinterpret_cast<const double2*>(v), b->d_off, b->d_poff,
                                                          b->d_rows, b->n_inst, b->n_total, h->n_pad, R, f32, ws.ta.p);
   KPM_CUDA_TRY(cudaGetLastError());
   KPM_CUDA_TRY(cudaMemcpyAsync(ws.vl.p, ws.ta.p, vb, cudaMemcpyDeviceToDevice, s));
+  if (dbl) {
+    KPM_TRY(half_norms(ws.ta.p, f32, h->n_pad, R, ws.vr.p, s));
+    // per (instance, vector) corrections, stored after the reduced sets: [n_inst][R]
+    const int K = (M + 1) / 2;
+    double* corr = reinterpret_cast<double*>(static_cast<double2*>(ws.red.p) + (size_t)2 * b->n_inst * R * (K + 1));
+    KPM_TRY(doubling_corr(ws.ta.p, ws.vr.p, f32, h->n_pad, R, b->d_poff, b->n_inst, corr, s));
+  }
   // the recursion: one graph launch (re-recorded if a workspace buffer moved)
-  const void* bufs[5] = {ws.ta.p, ws.tb.p, ws.vl.p, ws.part.p, b->mu_int.p};
+  const void* bufs[8] = {ws.ta.p, ws.tb.p, ws.vl.p, ws.part.p, b->mu_int.p, dbl ? ws.vr.p : nullptr,
+                         dbl ? ws.red.p : nullptr, (dbl && f32) ? ws.tc.p : nullptr};
   cudaGraphExec_t exec = nullptr;
   for (size_t i = 0; i < b->graphs.size(); ++i) {
     auto& g = b->graphs[i];
-    if (g.f32 == (int)f32 && g.R == R && g.M == M && g.kind == plan->kind) {
-      if (std::equal(bufs, bufs + 5, g.bufs)) {
+    if (g.f32 == (int)f32 && g.R == R && g.M == M && g.kind == plan->kind && g.dbl == (int)dbl) {
+      if (std::equal(bufs, bufs + 8, g.bufs)) {
         exec = g.exec;
       } else {
         cudaGraphExecDestroy(g.exec);
@@ -615,7 +677,8 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
       g.R = R;
       g.M = M;
       g.kind = plan->kind;
-      std::copy(bufs, bufs + 5, g.bufs);
+      g.dbl = (int)dbl;
+      std::copy(bufs, bufs + 8, g.bufs);
       g.exec = exec;
       b->graphs.push_back(g);
     }
@@ -623,6 +686,16 @@ int kpm_batch_moments(kpm_batch* b, int dtype, int R, int M, const double* v, do
   }
   KPM_CUDA_TRY(cudaMemcpyAsync(mu, b->mu_int.p, (size_t)b->n_inst * R * M * sizeof(double2), cudaMemcpyDeviceToDevice, s));
   return KPM_OK;
+}
+
+int kpm_batch_props(const kpm_batch* b, int* hermitian, int* doubling) {
+  if (!b) return KPM_ERR_INVALID_ARG;
+  return kpm_ell_props(b->op, hermitian, doubling);
+}
+
+int kpm_batch_set_doubling(kpm_batch* b, int on) {
+  if (!b) return KPM_ERR_INVALID_ARG;
+  return kpm_ell_set_doubling(b->op, on);
 }
 
 int kpm_batch_check(kpm_batch* b, void* stream) {

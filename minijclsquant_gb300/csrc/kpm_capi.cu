@@ -125,9 +125,11 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
     c.grid = grid_for(h, Rg, vpt_for(f32, Rg));
     cands.push_back(c);
   }
-  // the staged kernel serves one moment set; two-set calls use the grid-stride kernel
-  for (int kind = 1; kind <= 2 && sets == 1; ++kind)
+  // the staged kernel serves one moment set; two-set calls use the grid-stride kernel;
+  // doubled moments (sets == 3) the grid-stride and the producer-warp kernels
+  for (int kind = 1; kind <= 2 && sets != 2; ++kind)
     for (int U = 1; U <= 2; ++U) {
+      if (sets == 3 && kind == 1) continue;
       if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
       const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2)
                                        : staged_ctas_f64(h->is_real, Rg, U, h->L, 2))
@@ -154,17 +156,19 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
     KPM_TRY(ensure(ws.ta, vb));
     KPM_TRY(ensure(ws.tb, vb));
     KPM_TRY(ensure(ws.vl, vb));
-    if (sets == 2) KPM_TRY(ensure(ws.vr, vb));
-    KPM_TRY(ensure(ws.part, (size_t)kChunk * sets * max_grid * Rg * sizeof(double2)));
+    if (sets >= 2) KPM_TRY(ensure(ws.vr, vb));
+    KPM_TRY(ensure(ws.part, (size_t)kChunk * std::min(sets, 2) * max_grid * Rg * sizeof(double2)));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.ta.p, 0, vb, s));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.tb.p, 0, vb, s));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.vl.p, 0, vb, s));
-    if (sets == 2) KPM_CUDA_TRY(cudaMemsetAsync(ws.vr.p, 0, vb, s));
+    if (sets >= 2) KPM_CUDA_TRY(cudaMemsetAsync(ws.vr.p, 0, vb, s));
     StepParams p = base_params(h, f32);
     p.tcur = ws.ta.p;
     p.tout = ws.tb.p;
-    p.vl = ws.vl.p;
+    p.vl = sets == 3 ? nullptr : ws.vl.p;
     p.vl2 = sets == 2 ? ws.vr.p : nullptr;
+    p.dbl = sets == 3;
+    p.hv = sets == 3 ? ws.vr.p : nullptr;
     p.part = static_cast<double2*>(ws.part.p);
     cudaEvent_t e0, e1;
     KPM_CUDA_TRY(cudaEventCreate(&e0));
@@ -191,9 +195,321 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
   return KPM_OK;
 }
 
+// ---- doubling ----------------------------------------------------------------
+// For Hermitian H and DOS moments (v_l = v_r = v), T_{2k} = 2 T_k^2 - T_0 and
+// T_{2k+1} = 2 T_{k+1} T_k - T_1 give
+//   mu_{2k}   = 2 sum_i (|t_k,i|^2 - |v_i|^2 / 2),   mu_{2k+1} = 2 <t_{k+1}|t_k> - mu_1,
+// t_k = T_k v, so ceil(M/2) - 1 recursion steps deliver M moments.  Summing the
+// per-site differences |t_k,i|^2 - |v_i|^2/2 (terms of both signs) instead of
+// 2<t_k|t_k> - mu_0 keeps the rounding error at the level of the direct moments.
+// (Weisse et al., Rev. Mod. Phys. 78, 275 (2006), Sec. II.B.)
+
+bool use_doubling(const kpm_ell_s* h, int M) { return h->hermitian && h->doubling && M >= 4; }
+
+template <typename T2, typename T>
+__global__ void half_norms_kernel(const T2* __restrict__ v, int64_t count, T* __restrict__ hv) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    const T2 z = v[i];
+    hv[i] = T(0.5) * (z.x * z.x + z.y * z.y);
+  }
+}
+
+int half_norms(const void* packed, bool f32, int64_t n_pad, int Rg, void* hv, cudaStream_t s) {
+  const int64_t count = n_pad * Rg;
+  const int g = (int)std::min<int64_t>((count + 255) / 256, 65536);
+  if (f32)
+    half_norms_kernel<<<g, 256, 0, s>>>(static_cast<const float2*>(packed), count, static_cast<float*>(hv));
+  else
+    half_norms_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(packed), count, static_cast<double*>(hv));
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
+// Sets bit 0 of *flag unless H_ji == conj(H_ij) exactly for every stored entry
+// (duplicate slots of one column summed in slot order).
+template <bool REAL>
+__global__ void hermitian_check_kernel(const void* __restrict__ val, const int32_t* __restrict__ col, int64_t ld,
+                                       int64_t n, int L, unsigned* flag) {
+  const int64_t total = n * L;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t % n;
+    const int s = (int)(t / n);
+    const int64_t j = col[(int64_t)s * ld + row];
+    bool bad;
+    if (REAL) {
+      const double* v = static_cast<const double*>(val);
+      if (v[(int64_t)s * ld + row] == 0.0) continue;
+      double hij = 0.0, hji = 0.0;
+      for (int q = 0; q < L; ++q) {
+        if (col[(int64_t)q * ld + row] == j) hij += v[(int64_t)q * ld + row];
+        if (col[(int64_t)q * ld + j] == row) hji += v[(int64_t)q * ld + j];
+      }
+      bad = hij != hji;
+    } else {
+      const double2* v = static_cast<const double2*>(val);
+      const double2 x = v[(int64_t)s * ld + row];
+      if (x.x == 0.0 && x.y == 0.0) continue;
+      double2 hij = make_double2(0.0, 0.0), hji = make_double2(0.0, 0.0);
+      for (int q = 0; q < L; ++q) {
+        if (col[(int64_t)q * ld + row] == j) {
+          hij.x += v[(int64_t)q * ld + row].x;
+          hij.y += v[(int64_t)q * ld + row].y;
+        }
+        if (col[(int64_t)q * ld + j] == row) {
+          hji.x += v[(int64_t)q * ld + j].x;
+          hji.y += v[(int64_t)q * ld + j].y;
+        }
+      }
+      bad = hij.x != hji.x || hij.y != -hji.y;
+    }
+    if (bad) atomicOr(flag, 1u);
+  }
+}
+
+int check_hermitian(kpm_ell_s* h, cudaStream_t s) {
+  DevBuf flag;
+  KPM_TRY(ensure(flag, sizeof(unsigned)));
+  int rc = check_cuda(cudaMemsetAsync(flag.p, 0, sizeof(unsigned), s));
+  const int64_t total = h->n * (int64_t)h->L;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, (int64_t)h->sm_count * 16));
+  if (rc == KPM_OK) {
+    if (h->is_real)
+      hermitian_check_kernel<true><<<g, 256, 0, s>>>(h->val64, h->col, h->n_pad, h->n, h->L,
+                                                      static_cast<unsigned*>(flag.p));
+    else
+      hermitian_check_kernel<false><<<g, 256, 0, s>>>(h->val64, h->col, h->n_pad, h->n, h->L,
+                                                       static_cast<unsigned*>(flag.p));
+    rc = check_cuda(cudaGetLastError());
+  }
+  unsigned hf = 1;
+  if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(&hf, flag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  if (rc == KPM_OK) rc = check_cuda(cudaStreamSynchronize(s));
+  release(flag);
+  if (rc == KPM_OK) h->hermitian = hf == 0u ? 1 : 0;
+  return rc;
+}
+
+// corr[seg][r] = sum over the segment's rows of (2 hv_i - |v_i|^2) in FP64, from the
+// working-precision values the recursion uses.  hv is |v|^2/2 rounded to the working
+// precision; for unit-modulus vectors every |v_i|^2 is close to 1, where rounding is
+// not symmetric, so these per-site roundings add up coherently.  Adding corr to
+// every even moment removes them exactly.
+template <typename T2, typename T>
+__global__ void doubling_corr_kernel(const T2* __restrict__ v, const T* __restrict__ hv, int Rg,
+                                     const int64_t* __restrict__ seg_begin, int nseg, int64_t n_pad,
+                                     double* __restrict__ corr) {
+  const int r = blockIdx.x, sg = blockIdx.y;
+  const int64_t b = seg_begin ? seg_begin[sg] : 0;
+  const int64_t e = seg_begin ? (sg + 1 < nseg ? seg_begin[sg + 1] : n_pad) : n_pad;
+  double acc = 0.0;
+  for (int64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+    const T2 z = v[i * Rg + r];
+    const double x = (double)z.x, y = (double)z.y;
+    acc += 2.0 * (double)hv[i * Rg + r] - (x * x + y * y);
+  }
+  __shared__ double sh[256];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) corr[(int64_t)sg * Rg + r] = sh[0];
+}
+
+int doubling_corr(const void* packed, const void* hv, bool f32, int64_t n_pad, int Rg, const int64_t* seg_begin,
+                  int nseg, double* corr, cudaStream_t s) {
+  dim3 g(Rg, nseg);
+  if (f32)
+    doubling_corr_kernel<<<g, 256, 0, s>>>(static_cast<const float2*>(packed), static_cast<const float*>(hv), Rg,
+                                           seg_begin, nseg, n_pad, corr);
+  else
+    doubling_corr_kernel<<<g, 256, 0, s>>>(static_cast<const double2*>(packed), static_cast<const double*>(hv), Rg,
+                                           seg_begin, nseg, n_pad, corr);
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
+// mu_1 = <v|H v> in FP64 for a complex64 start vector v (the float values the
+// recursion starts from), with the FP64 operator.  Doubled odd moments are
+// 2<t_{k+1}|t_k> - mu_1: an error in mu_1 enters every one of them alike, so the
+// complex64 first step's own <v|t_1> (t_1 rounded to float) is not used there.
+// part[seg][split][r] partial sums, split blocks per (vector, segment).
+template <bool REAL>
+__global__ void mu1_exact_kernel(const void* __restrict__ val64, const int32_t* __restrict__ col, int64_t ld,
+                                 int L, const float2* __restrict__ v, int Rg, const int64_t* __restrict__ seg_begin,
+                                 int nseg, int64_t n_pad, int split, double2* __restrict__ part) {
+  const int r = blockIdx.x, sg = blockIdx.y, sp = blockIdx.z;
+  const int64_t b = seg_begin ? seg_begin[sg] : 0;
+  const int64_t e = seg_begin ? (sg + 1 < nseg ? seg_begin[sg + 1] : n_pad) : n_pad;
+  double ar = 0.0, ai = 0.0;
+  for (int64_t i = b + (int64_t)sp * blockDim.x + threadIdx.x; i < e; i += (int64_t)split * blockDim.x) {
+    double hr = 0.0, hi = 0.0;  // (2H v)_i
+    for (int q = 0; q < L; ++q) {
+      const int64_t j = col[(int64_t)q * ld + i];
+      const float2 x = v[j * Rg + r];
+      if (REAL) {
+        const double h = static_cast<const double*>(val64)[(int64_t)q * ld + i];
+        hr = fma(h, (double)x.x, hr);
+        hi = fma(h, (double)x.y, hi);
+      } else {
+        const double2 h = static_cast<const double2*>(val64)[(int64_t)q * ld + i];
+        hr = fma(h.x, (double)x.x, fma(-h.y, (double)x.y, hr));
+        hi = fma(h.x, (double)x.y, fma(h.y, (double)x.x, hi));
+      }
+    }
+    const float2 w = v[i * Rg + r];
+    ar += 0.5 * ((double)w.x * hr + (double)w.y * hi);  // conj(v_i) * (H v)_i
+    ai += 0.5 * ((double)w.x * hi - (double)w.y * hr);
+  }
+  __shared__ double shr[256], shi[256];
+  shr[threadIdx.x] = ar;
+  shi[threadIdx.x] = ai;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) {
+      shr[threadIdx.x] += shr[threadIdx.x + w];
+      shi[threadIdx.x] += shi[threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[((int64_t)sg * split + sp) * Rg + r] = make_double2(shr[0], shi[0]);
+}
+
+// out[(row0 + seg * Rg + r) * stride + 1] = sum over splits, fixed order
+__global__ void mu1_store_kernel(const double2* __restrict__ part, int Rg, int nseg, int split, double2* out,
+                                 int64_t stride, int64_t row0) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nseg * Rg) return;
+  const int sg = (int)(t / Rg), r = (int)(t % Rg);
+  double2 acc = make_double2(0.0, 0.0);
+  for (int sp = 0; sp < split; ++sp) {
+    const double2 x = part[((int64_t)sg * split + sp) * Rg + r];
+    acc.x += x.x;
+    acc.y += x.y;
+  }
+  out[(row0 + (int64_t)sg * Rg + r) * stride + 1] = acc;
+}
+
+int mu1_exact(const kpm_ell_s* h, const void* packed_f32, int Rg, const int64_t* seg_begin, int nseg, double2* out,
+              int64_t stride, int64_t row0, DevBuf& scratch, cudaStream_t s) {
+  const int split = (int)std::max<int64_t>(1, std::min<int64_t>(64, (int64_t)h->sm_count * 4 / ((int64_t)Rg * nseg)));
+  KPM_TRY(ensure(scratch, (size_t)nseg * split * Rg * sizeof(double2)));
+  dim3 g(Rg, nseg, split);
+  double2* part = static_cast<double2*>(scratch.p);
+  const float2* v = static_cast<const float2*>(packed_f32);
+  if (h->is_real)
+    mu1_exact_kernel<true><<<g, 256, 0, s>>>(h->val64, h->col, h->n_pad, h->L, v, Rg, seg_begin, nseg, h->n_pad,
+                                             split, part);
+  else
+    mu1_exact_kernel<false><<<g, 256, 0, s>>>(h->val64, h->col, h->n_pad, h->L, v, Rg, seg_begin, nseg, h->n_pad,
+                                              split, part);
+  KPM_CUDA_TRY(cudaGetLastError());
+  const int64_t total = (int64_t)nseg * Rg;
+  mu1_store_kernel<<<(int)((total + 255) / 256), 256, 0, s>>>(part, Rg, nseg, split, out, stride, row0);
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
+// mu[row0 + r][j], j = 2 .. M-1, from the reduced sets [rows][K + 1]:
+// j = 2k: 2 d[k + 1] + corr[r];  j = 2k + 1: 2 b[k + 1] - mu[.][1].
+__global__ void assemble_doubled_kernel(const double2* __restrict__ rb, const double2* __restrict__ rd,
+                                        const double* __restrict__ corr, int rows, int K, int M, double2* mu,
+                                        int64_t stride, int64_t row0) {
+  const int64_t per = M - 2;
+  const int64_t total = (int64_t)rows * per;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / per);
+    const int j = 2 + (int)(t % per);
+    double2* out = mu + (row0 + r) * stride;
+    if ((j & 1) == 0) {
+      const double2 d = rd[(int64_t)r * (K + 1) + j / 2 + 1];
+      out[j] = make_double2(2.0 * d.x + corr[r], 2.0 * d.y);
+    } else {
+      const double2 b = rb[(int64_t)r * (K + 1) + (j + 1) / 2];
+      const double2 m1 = out[1];
+      out[j] = make_double2(2.0 * b.x - m1.x, 2.0 * b.y - m1.y);
+    }
+  }
+}
+
+int assemble_doubled(const double2* red_b, const double2* red_d, const double* corr, int rows, int K, int M,
+                     double2* mu, int64_t mu_row_stride, int64_t mu_row0, cudaStream_t s) {
+  if (M <= 2) return KPM_OK;
+  const int64_t total = (int64_t)rows * (M - 2);
+  const int g = (int)std::min<int64_t>((total + 255) / 256, 4096);
+  assemble_doubled_kernel<<<g, 256, 0, s>>>(red_b, red_d, corr, rows, K, M, mu, mu_row_stride, mu_row0);
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
+// DOS moments of one group by doubling: the first step gives mu_0, mu_1; steps
+// m = 2 .. K = ceil(M/2) produce t_m and the sets <t_m|t_{m-1}>, sum(|t_{m-1}|^2 - hv).
+int moments_group_doubled(kpm_ell_s* h, bool f32, int r0, int Rg, int M, const double* v, int R, double* mu,
+                          cudaStream_t s) {
+  const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+  StepConfig cfg;
+  KPM_TRY(step_config(h, f32, Rg, 3, s, &cfg));
+  const int grid = cfg.grid;
+  const int K = (M + 1) / 2;
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  KPM_TRY(ensure(ws.vr, vb));  // |v|^2 / 2 (half of vb used)
+  const int64_t step_stride = (int64_t)2 * grid * Rg;
+  KPM_TRY(ensure(ws.part, (size_t)kChunk * step_stride * sizeof(double2)));
+  KPM_TRY(ensure(ws.red, (size_t)2 * Rg * (K + 1) * sizeof(double2) + (size_t)Rg * sizeof(double)));
+  KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, f32, ws.ta.p, s));
+  KPM_CUDA_TRY(cudaMemcpyAsync(ws.vl.p, ws.ta.p, vb, cudaMemcpyDeviceToDevice, s));
+  KPM_TRY(half_norms(ws.ta.p, f32, h->n_pad, Rg, ws.vr.p, s));
+  double* corr = reinterpret_cast<double*>(static_cast<double2*>(ws.red.p) + (size_t)2 * Rg * (K + 1));
+  KPM_TRY(doubling_corr(ws.ta.p, ws.vr.p, f32, h->n_pad, Rg, nullptr, 1, corr, s));
+  double2* part = static_cast<double2*>(ws.part.p);
+  StepParams p = base_params(h, f32);
+  // m = 1 and the moment of T_0, direct: mu_0 = <v|v>, mu_1 = <v|H v>
+  p.vl = ws.vl.p;
+  p.part_step_stride = (int64_t)grid * Rg;
+  p.tcur = ws.ta.p;
+  p.tout = ws.tb.p;
+  p.part = part;
+  KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_FIRST, EPI_STORE | EPI_MOM1, p, grid, s));
+  double* outs_first[2] = {mu, mu};
+  KPM_TRY(reduce_partials(part, 2, 1, grid, Rg, outs_first, R, r0, M, 0, s));
+  if (f32)  // mu_1 exactly for the float start vector (enters every odd moment)
+    KPM_TRY(mu1_exact(h, ws.vl.p, Rg, nullptr, 1, reinterpret_cast<double2*>(mu), M, r0, ws.tc, s));
+  // later steps: two sets per step
+  p.vl = nullptr;
+  p.dbl = 1;
+  p.hv = ws.vr.p;
+  double2* rb = static_cast<double2*>(ws.red.p);
+  double2* rd = rb + (size_t)Rg * (K + 1);
+  double* outs[2] = {reinterpret_cast<double*>(rb), reinterpret_cast<double*>(rd)};
+  void* tprev = ws.ta.p;
+  void* tcur = ws.tb.p;
+  int m0 = 2;
+  cudaEvent_t ev = nullptr;
+  if (K >= 2) KPM_TRY(prof_begin(h, s, &ev));
+  for (int m = 2; m <= K; ++m) {
+    if (m - m0 == kChunk) {
+      KPM_TRY(reduce_partials(part, kChunk, 2, grid, Rg, outs, Rg, 0, K + 1, m0, s));
+      m0 = m;
+    }
+    p.tcur = tcur;
+    p.tout = tprev;
+    p.part = part + (int64_t)(m - m0) * step_stride;
+    KPM_TRY(launch_next(f32, h->is_real, Rg, cfg, p, s));
+    std::swap(tprev, tcur);
+  }
+  if (K >= 2) KPM_TRY(prof_end(h, s, ev, K - 1));
+  KPM_TRY(reduce_partials(part, K + 1 - m0, 2, grid, Rg, outs, Rg, 0, K + 1, m0, s));
+  return assemble_doubled(rb, rd, corr, Rg, K, M, reinterpret_cast<double2*>(mu), M, r0, s);
+}
+
 // Moments for one group of Rg <= 8 vectors starting at r0.
 int moments_group(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const double* v_r, const double* v_l,
                   double* mu, double* mu_rr, cudaStream_t s) {
+  if (!v_l && !mu_rr && use_doubling(h, M)) return moments_group_doubled(h, f32, r0, Rg, M, v_r, R, mu, s);
   const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
   const int sets = mu_rr ? 2 : 1;
   StepConfig cfg;
@@ -299,7 +615,7 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
                    unsigned flags, void* stream) {
   if (!out || !data || !indices || n_rows < 1 || len_row < 1) return KPM_ERR_INVALID_ARG;
   if (n_rows > (int64_t)INT32_MAX) return KPM_ERR_SHAPE;
-  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG)) return KPM_ERR_INVALID_ARG;
+  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG | KPM_FLAG_DOUBLING)) return KPM_ERR_INVALID_ARG;
   *out = nullptr;
   cudaStream_t s = as_stream(stream);
   kpm_ell_s* h = new kpm_ell_s();
@@ -379,6 +695,8 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
   release(stage_data);
   release(stage_idx);
   release(flag_buf);
+  h->doubling = (flags & KPM_FLAG_DOUBLING) ? 1 : 0;
+  if ((st = check_hermitian(h, s)) != KPM_OK) return fail(st);
   *out = h;
   return KPM_OK;
 }
@@ -428,10 +746,15 @@ int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M) {
   KPM_TRY(ensure(ws.tb, vb));
   KPM_TRY(ensure(ws.vl, vb));
   KPM_TRY(ensure(ws.vr, vb));
-  StepConfig c1, c2;
+  StepConfig c1, c2, c3;
   KPM_TRY(step_config(h, f32, Rg, 1, nullptr, &c1));
   KPM_TRY(step_config(h, f32, Rg, 2, nullptr, &c2));
-  const int grid = std::max(c1.grid, c2.grid);
+  int grid = std::max(c1.grid, c2.grid);
+  if (use_doubling(h, M)) {
+    KPM_TRY(step_config(h, f32, Rg, 3, nullptr, &c3));
+    grid = std::max(grid, c3.grid);
+    KPM_TRY(ensure(ws.red, (size_t)2 * Rg * ((M + 1) / 2 + 1) * sizeof(double2)));
+  }
   KPM_TRY(ensure(ws.part, (size_t)kChunk * 2 * grid * Rg * sizeof(double2)));
   KPM_CUDA_TRY(cudaDeviceSynchronize());
   return KPM_OK;
@@ -580,11 +903,24 @@ int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_t
   const int Rg = pow2_group(R);
   if (dtype == KPM_C64) KPM_TRY(ensure_f32_values(h, nullptr));
   StepConfig cfg;
-  KPM_TRY(step_config(h, dtype == KPM_C64, Rg, 1, nullptr, &cfg));
+  KPM_TRY(step_config(h, dtype == KPM_C64, Rg, use_doubling(h, 4) ? 3 : 1, nullptr, &cfg));
   if (kind) *kind = cfg.kind;
   if (rows_per_thread) *rows_per_thread = cfg.U;
   if (grid) *grid = cfg.grid;
   if (step_us) *step_us = cfg.us;
+  return KPM_OK;
+}
+
+int kpm_ell_props(const kpm_ell* h, int* hermitian, int* doubling) {
+  if (!h) return KPM_ERR_INVALID_ARG;
+  if (hermitian) *hermitian = h->hermitian;
+  if (doubling) *doubling = use_doubling(h, 4) ? 1 : 0;
+  return KPM_OK;
+}
+
+int kpm_ell_set_doubling(kpm_ell* h, int on) {
+  if (!h) return KPM_ERR_INVALID_ARG;
+  h->doubling = on ? 1 : 0;
   return KPM_OK;
 }
 

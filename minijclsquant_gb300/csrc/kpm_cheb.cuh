@@ -280,6 +280,8 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
   const Raw* __restrict__ vl = static_cast<const Raw*>(p.vl);
   const Raw* __restrict__ vl2 = static_cast<const Raw*>(p.vl2);
   const bool mom2 = MOM && (vl2 != nullptr);
+  // doubling: set 0 <T_{m}|T_{m-1}> (own row of tcur), set 1 sum (|T_{m-1}|^2 - hv)
+  const bool dbl = MOM && MODE == MODE_NEXT && p.dbl != 0;
   const int L = p.L;
   const int64_t ld = p.ld;
 
@@ -363,7 +365,30 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
     }
     if (STORE) tout[vi] = pack(acc);
 
-    if (MOM) {
+    if (MOM && dbl) {
+      Cx<T, VPT> own;
+      unpack(__ldg(tcur + vi), own);
+      const T* hv = static_cast<const T*>(p.hv) + vi * VPT;
+#pragma unroll
+      for (int k = 0; k < VPT; ++k) {
+        const T hk = __ldg(hv + k);
+        if (F32) {
+          cdot_acc(f1r[k], f1i[k], acc.re[k], acc.im[k], own.re[k], own.im[k]);
+          f2r[k] += fmaf(own.re[k], own.re[k], fmaf(own.im[k], own.im[k], -hk));
+        } else {
+          cdot_acc(m1r[k], m1i[k], acc.re[k], acc.im[k], own.re[k], own.im[k]);
+          m2r[k] += fma(own.re[k], own.re[k], fma(own.im[k], own.im[k], -hk));
+        }
+      }
+      if (F32 && ++pending == kFlush) {
+        pending = 0;
+#pragma unroll
+        for (int k = 0; k < VPT; ++k) {
+          m1r[k] += (double)f1r[k]; m1i[k] += (double)f1i[k]; f1r[k] = f1i[k] = T(0);
+          m2r[k] += (double)f2r[k]; f2r[k] = T(0);
+        }
+      }
+    } else if (MOM) {
       Cx<T, VPT> l;
       unpack(__ldg(vl + vi), l);
       Cx<T, VPT> l2;
@@ -438,7 +463,7 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
       }
     }
     const int64_t set_stride = (int64_t)gridDim.x * R;
-    const int sets = mom2 ? 2 : 1;
+    const int sets = (mom2 || dbl) ? 2 : 1;
     // partial layout for one step: [sets][grid][R]
     if (MODE == MODE_FIRST) {
       double2* p0 = p.part;                       // step m = 0

@@ -33,6 +33,14 @@ constexpr int kChunk = 128;       // recursion steps whose moment partials are b
 
 void set_last_cuda_error(cudaError_t e);
 
+// Status of a CUDA runtime result (records it and clears the sticky error state).
+inline int check_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return KPM_OK;
+  set_last_cuda_error(e);
+  (void)cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? KPM_ERR_OOM : KPM_ERR_CUDA;
+}
+
 #define KPM_CUDA_TRY(expr)                                  \
   do {                                                      \
     cudaError_t kpm_e_ = (expr);                            \
@@ -63,6 +71,7 @@ struct Workspace {
   DevBuf part;             // per-CTA moment partials [kChunk][sets][grid][R] double2
   DevBuf coef;             // small device staging (coefficients)
   DevBuf ckpt, seg, grad;  // adjoint: checkpoint pairs, recomputed segment, per-slot gradient
+  DevBuf red;              // doubling: reduced sets [2][R][K + 1], then the per-vector corrections
 };
 
 // Kernel choice for the recursion step of one (precision, R group, moment sets).
@@ -96,6 +105,9 @@ struct kpm_ell_s {
   std::vector<std::pair<int, kpm::StepConfig>> tuned;
   // the forward pass the next kpm_adjoint_backward differentiates
   int adj_R = 0, adj_M = 0, adj_ckpt = 0;
+  // H == H^dagger, checked on the device at creation; doubling allowed for DOS moments
+  int hermitian = 0;
+  int doubling = 0;  // requested (KPM_FLAG_DOUBLING / kpm_ell_set_doubling)
 };
 
 namespace kpm {
@@ -125,6 +137,13 @@ struct StepParams {
   const void* tprev;      // grid-stride MODE_NEXT: read T_{m-1} here instead of tout (out of place)
   const int* tile_inst;   // per_tile: instance of every tile
   const int* seg_base;    // per_tile: first partial slot of every CTA
+  // Doubling (Hermitian H, DOS moments): the step producing t_{k+1} = T_{k+1} v
+  // accumulates two sets instead of <v_l|T_{m+1}>: set 0 <t_{k+1}|t_k> and set 1
+  // sum_i (|t_k,i|^2 - hv_i) with hv = |v|^2 / 2, so that mu_{2k+1} = 2 set0 - mu_1
+  // and mu_{2k} = 2 set1.  t_k is the own row of tcur.
+  int dbl;
+  const void* hv;         // dbl: |v|^2 / 2, real, [n_pad][R] (working precision)
+  int64_t part_set_stride;  // per_tile with two sets: elements between the sets' slot blocks
 };
 
 // Launch helpers implemented per precision (kpm_cheb_c128.cu, kpm_cheb_c64.cu).
@@ -150,6 +169,17 @@ StepParams base_params(kpm_ell_s* h, bool f32);
 int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
 int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s);
 int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out);
+// Doubling: whether a DOS moment call on h uses it; |v|^2 / 2 of a packed set; the
+// Hermitian check run at creation; the assembly of mu from the reduced sets.
+bool use_doubling(const kpm_ell_s* h, int M);
+int half_norms(const void* packed, bool f32, int64_t n_pad, int Rg, void* hv, cudaStream_t s);
+int check_hermitian(kpm_ell_s* h, cudaStream_t s);
+int doubling_corr(const void* packed, const void* hv, bool f32, int64_t n_pad, int Rg, const int64_t* seg_begin,
+                  int nseg, double* corr, cudaStream_t s);
+int mu1_exact(const kpm_ell_s* h, const void* packed_f32, int Rg, const int64_t* seg_begin, int nseg, double2* out,
+              int64_t stride, int64_t row0, DevBuf& scratch, cudaStream_t s);
+int assemble_doubled(const double2* red_b, const double2* red_d, const double* corr, int rows, int K, int M,
+                     double2* mu, int64_t mu_row_stride, int64_t mu_row0, cudaStream_t s);
 int check_dtype(int dtype);
 
 // Rows per tile of the staged kernel (complex64 packs two vectors per thread).

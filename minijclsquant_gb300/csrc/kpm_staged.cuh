@@ -50,6 +50,7 @@ struct TileCopy {
   uint32_t col_slab;   // bytes of one column slab (TILE * 4)
   uint32_t val_slab;   // bytes of one value slab
   uint32_t vec_slab;   // bytes of one vector tile
+  uint32_t vl_slab;    // bytes of the left-vector (or half-norm) tile
   uint32_t col_b, val_b;  // stage offsets
   uint32_t tx_bytes;
 };
@@ -66,7 +67,9 @@ static __device__ __noinline__ void issue_tile(const TileCopy& tc, unsigned char
              bar, pol);
   const int64_t voff = row0 * vec_bytes_per_row;
   bulk_g2s(stage + tc.col_b + tc.val_b, tc.old + voff, tc.vec_slab, bar, pol);
-  if (tc.vl) bulk_g2s(stage + tc.col_b + tc.val_b + tc.vec_slab, tc.vl + voff, tc.vec_slab, bar, pol);
+  if (tc.vl)
+    bulk_g2s(stage + tc.col_b + tc.val_b + tc.vec_slab, tc.vl + row0 * (int64_t)(tc.vl_slab / tile), tc.vl_slab, bar,
+             pol);
 }
 
 template <typename T, bool REAL, int TPR, int VPT, int U>
@@ -120,6 +123,7 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
     tc.col_slab = TILE * 4;
     tc.val_slab = (uint32_t)(TILE * sizeof(MV));
     tc.vec_slab = vec_b;
+    tc.vl_slab = vec_b;
     tc.col_b = col_b;
     tc.val_b = val_b;
     tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + 2 * vec_b;

@@ -16,6 +16,9 @@
 // reduction over the compute warps alone (named barrier 1).  With p.vl null the
 // step stores T_{m+1} only (no left vector is copied, no moments), and with
 // p.tprev set T_{m-1} is read from there (out of place) instead of from tout.
+// With p.dbl (doubling) the producer stages |v|^2 / 2 in place of the left
+// vector and the two moment sets <T_{m+1}|T_m>, sum (|T_m|^2 - |v|^2 / 2) are
+// accumulated (T_m's own row read from tcur).
 //
 // Every wait is bounded.  A compute warp whose wait runs out records
 // KPM_ERR_TIMEOUT and stops computing but still takes part in the named
@@ -86,9 +89,11 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
       tc.col_slab = TILE * 4;
       tc.val_slab = (uint32_t)(TILE * sizeof(MV));
       tc.vec_slab = vec_b;
+      tc.vl_slab = p.dbl ? (uint32_t)(TILE * R * sizeof(T)) : vec_b;
+      if (p.dbl) tc.vl = static_cast<const unsigned char*>(p.hv);
       tc.col_b = col_b;
       tc.val_b = val_b;
-      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + (p.vl ? 2 : 1) * vec_b;
+      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + vec_b + (tc.vl ? tc.vl_slab : 0);
       int issued = 0;
       for (int k = 0; k < my_count; ++k) {
         const int st = k % kWsStages;
@@ -109,21 +114,38 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
 
   int seg = p.per_tile ? p.seg_base[blockIdx.x] : 0;
   int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
-  const bool mom = p.vl != nullptr;
+  const bool dbl = p.dbl != 0;
+  const bool mom = p.vl != nullptr || dbl;
+  const int64_t set_stride = p.per_tile ? p.part_set_stride : (int64_t)gridDim.x * R;
 
   const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
   Raw* tout = static_cast<Raw*>(p.tout);
   const int sub = threadIdx.x % TPR;
   const int rl = threadIdx.x / TPR;
-  double mr[VPT], mi[VPT];
-  T fr[VPT], fi[VPT];
+  double mr[VPT], mi[VPT], mr2[VPT], mi2[VPT];
+  T fr[VPT], fi[VPT], fr2[VPT];
 #pragma unroll
   for (int q = 0; q < VPT; ++q) {
-    mr[q] = mi[q] = 0.0;
-    fr[q] = fi[q] = T(0);
+    mr[q] = mi[q] = mr2[q] = mi2[q] = 0.0;
+    fr[q] = fi[q] = fr2[q] = T(0);
   }
   int pending = 0;
   bool dead = false;
+  auto fold = [&]() {
+#pragma unroll
+    for (int q = 0; q < VPT; ++q) {
+      mr[q] += (double)fr[q];
+      mi[q] += (double)fi[q];
+      mr2[q] += (double)fr2[q];
+      fr[q] = fi[q] = fr2[q] = T(0);
+    }
+  };
+  auto flush_sets = [&](double2* dst) {
+    block_reduce_store<TPR, VPT>(mr, mi, dst, red, true);
+    if (dbl) block_reduce_store<TPR, VPT>(mr2, mi2, dst + set_stride, red, true);
+#pragma unroll
+    for (int q = 0; q < VPT; ++q) mr[q] = mi[q] = mr2[q] = 0.0;
+  };
 
   for (int k = 0; k < my_count; ++k) {
     const int st = k % kWsStages;
@@ -173,33 +195,51 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
         }
       }
       Cx<T, VPT> acc[U], l[U];
+      T hvs[U][VPT];
 #pragma unroll
       for (int u = 0; u < U; ++u) {
         acc[u] = finish(accum[u]);
-        if (mom) unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
+        if (dbl) {
+          const T* shv = reinterpret_cast<const T*>(svl) + ((u * RPB + rl) * TPR + sub) * VPT;
+#pragma unroll
+          for (int q = 0; q < VPT; ++q) hvs[u][q] = shv[q];
+        } else if (mom) {
+          unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
+        }
       }
       // the stage is no longer read: hand it back to the producer
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[st]);
 #pragma unroll
       for (int u = 0; u < U; ++u) {
-        tout[(row0 + u * RPB + rl) * TPR + sub] = pack(acc[u]);
+        const int64_t vi = (row0 + u * RPB + rl) * TPR + sub;
+        tout[vi] = pack(acc[u]);
         if (!mom) continue;
+        if (dbl) {
+          Cx<T, VPT> own;  // T_m at this row
+          unpack(__ldg(tcur + vi), own);
 #pragma unroll
-        for (int q = 0; q < VPT; ++q) {
-          if (F32)
-            cdot_acc(fr[q], fi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
-          else
-            cdot_acc(mr[q], mi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+          for (int q = 0; q < VPT; ++q) {
+            if (F32) {
+              cdot_acc(fr[q], fi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
+              fr2[q] += fmaf(own.re[q], own.re[q], fmaf(own.im[q], own.im[q], -hvs[u][q]));
+            } else {
+              cdot_acc(mr[q], mi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
+              mr2[q] += fma(own.re[q], own.re[q], fma(own.im[q], own.im[q], -hvs[u][q]));
+            }
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < VPT; ++q) {
+            if (F32)
+              cdot_acc(fr[q], fi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+            else
+              cdot_acc(mr[q], mi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+          }
         }
         if (F32 && ++pending == kFlush) {
           pending = 0;
-#pragma unroll
-          for (int q = 0; q < VPT; ++q) {
-            mr[q] += (double)fr[q];
-            mi[q] += (double)fi[q];
-            fr[q] = fi[q] = T(0);
-          }
+          fold();
         }
       }
     }
@@ -207,17 +247,10 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
       const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
       if (next_inst != cur_inst) {
         if (F32) {
-#pragma unroll
-          for (int q = 0; q < VPT; ++q) {
-            mr[q] += (double)fr[q];
-            mi[q] += (double)fi[q];
-            fr[q] = fi[q] = T(0);
-          }
+          fold();
           pending = 0;
         }
-        block_reduce_store<TPR, VPT>(mr, mi, p.part + (int64_t)seg * R, red, true);
-#pragma unroll
-        for (int q = 0; q < VPT; ++q) mr[q] = mi[q] = 0.0;
+        flush_sets(p.part + (int64_t)seg * R);
         ++seg;
         cur_inst = next_inst;
       }
@@ -225,14 +258,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
   }
 
   if (!p.per_tile && mom) {
-    if (F32) {
-#pragma unroll
-      for (int q = 0; q < VPT; ++q) {
-        mr[q] += (double)fr[q];
-        mi[q] += (double)fi[q];
-      }
-    }
-    block_reduce_store<TPR, VPT>(mr, mi, p.part + (int64_t)blockIdx.x * R, red, true);
+    if (F32) fold();
+    flush_sets(p.part + (int64_t)blockIdx.x * R);
   }
 }
 

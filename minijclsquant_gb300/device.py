@@ -41,7 +41,9 @@ def _as_device_c128(x, n: int | None = None) -> torch.Tensor:
 class DeviceELL:
     """A libkpm operator: SoA ELL on the GPU (values doubled, rows padded)."""
 
-    def __init__(self, data, indices, len_row: int, n_rows: int | None = None):
+    def __init__(self, data, indices, len_row: int, n_rows: int | None = None, *, doubling: bool = False):
+        """doubling=True: DOS moments of a Hermitian operator use the doubling
+        identity (ceil(M/2) - 1 recursion steps instead of M - 2)."""
         _require_cuda()
         lib = _capi.lib()
         data_is_dev = isinstance(data, torch.Tensor) and data.is_cuda
@@ -67,6 +69,8 @@ class DeviceELL:
             raise ValueError("ELL arrays hold %d entries, expected %d x %d" % (count, n, len_row))
         if (not data_is_dev) and ix.size != count:
             raise ValueError("data and indices differ in length")
+        if doubling:
+            flags |= _capi.KPM_FLAG_DOUBLING
         handle = ctypes.c_void_p()
         torch.cuda.synchronize()
         st = lib.kpm_ell_create(ctypes.byref(handle), n, len_row, dptr, iptr, flags, _stream_ptr())
@@ -78,6 +82,23 @@ class DeviceELL:
         is_real = ctypes.c_int()
         lib.kpm_ell_info(self._h, ctypes.byref(info_n), None, ctypes.byref(is_real), None)
         self.is_real = bool(is_real.value)
+
+    @property
+    def hermitian(self) -> bool:
+        """H == H^dagger exactly (checked on the device at creation)."""
+        h = ctypes.c_int()
+        _capi.check(_capi.lib().kpm_ell_props(self._h, ctypes.byref(h), None), "kpm_ell_props")
+        return bool(h.value)
+
+    @property
+    def doubling(self) -> bool:
+        """Whether DOS moment calls use the doubling identity."""
+        d = ctypes.c_int()
+        _capi.check(_capi.lib().kpm_ell_props(self._h, None, ctypes.byref(d)), "kpm_ell_props")
+        return bool(d.value)
+
+    def set_doubling(self, on: bool):
+        _capi.check(_capi.lib().kpm_ell_set_doubling(self._h, int(bool(on))), "kpm_ell_set_doubling")
 
     @property
     def handle(self):

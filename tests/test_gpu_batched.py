@@ -56,16 +56,22 @@ def test_batched_graph_replay_is_deterministic(cuda_lib):
 KINDS = {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2), "ws1": (2, 1), "ws2": (2, 2)}
 
 
+@pytest.mark.parametrize("doubled", [False, True])
 @pytest.mark.parametrize("kernel", list(KINDS))
 @pytest.mark.parametrize("dtype,R", [("c128", 4), ("c64", 2), ("c64", 8)])
-def test_batched_kernel_variants_agree(cuda_lib, monkeypatch, kernel, dtype, R):
+def test_batched_kernel_variants_agree(cuda_lib, monkeypatch, kernel, dtype, R, doubled):
     """Every kernel the batched autotuner can pick, forced, against the oracle per
-    instance (complex128 at 1e-10 per order; complex64 at its own precision)."""
+    instance (complex128 at 1e-10 per order; complex64 at its own precision), for the
+    direct recursion and for doubled moments."""
     from minijclsquant_gb300 import batched
 
+    if doubled and kernel.startswith("staged"):
+        pytest.skip("doubled moments run on the grid-stride and producer-warp kernels")
     monkeypatch.setenv("KPM_STEP_KERNEL", kernel)
     datas, idxs, L, _, _ = _ensemble(6, (3, 70), seed=5)  # 18 .. 9800 sites: tiny and multi-tile instances
     B = batched.BatchedELL(datas, idxs, L)
+    B.set_doubling(doubled)
+    assert B.doubling == doubled
     v = batched.ensemble_vectors(B.rows, R)
     mu = B.moments(90, v, dtype=dtype)
     cfg = B.step_config(dtype, R)

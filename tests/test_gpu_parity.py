@@ -221,11 +221,15 @@ def test_long_recursion_crosses_moment_chunks(cuda_lib):
         assert oracle.moment_tolerance_ok(mu, ref, REL)[0], M
 
 
+@pytest.mark.parametrize("doubled", [False, True])
 @pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2", "ws1", "ws2"])
 @pytest.mark.parametrize("dtype,R", [("c128", 8), ("c128", 1), ("c128", 4), ("c64", 2), ("c64", 8), ("c64", 1)])
-def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R):
+def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R, doubled):
     """Each recursion-step kernel the autotuner can pick, forced, against the oracle
-    (complex128 at 1e-10; complex64 at its own precision)."""
+    (complex128 at 1e-10; complex64 at its own precision), for the direct recursion
+    and for doubled moments (which the staged kernels do not serve)."""
+    if doubled and kernel.startswith("staged"):
+        pytest.skip("doubled moments run on the grid-stride and producer-warp kernels")
     from minijclsquant_gb300 import _capi, device, lattice
     from minijclsquant_gb300.modifiers import modifier_bounds
     from minijclsquant_gb300.observables import random_vector_generator
@@ -233,7 +237,8 @@ def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R):
     monkeypatch.setenv("KPM_STEP_KERNEL", kernel)
     H = lattice.honeycomb(40, 36, t=-2.7, W=0.7, seed=5)  # 2880 sites: several tiles, ragged last CTA
     Hk = H.modifier(modifier_bounds)
-    op = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row)
+    op = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row, doubling=doubled)
+    assert op.doubling == doubled
     n = op.n
     vs = np.stack([random_vector_generator(n, 40 + r) for r in range(R)])
     mu = device.cheb_moments(op, 150, vs, dtype=dtype)

@@ -706,6 +706,34 @@ def run_ours(a):
             "max_abs_diff_vs_direct_over_mu0": float(np.max(np.abs(mu_dbl.cpu().numpy() - mu_h))
                                                      / np.max(np.abs(mu_h[:, 0]))),
             "note": "opt-in (KPM_FLAG_DOUBLING); value counts site-steps per moment delivered, N R (M-1)"}
+    if a.dtype == "c128":
+        # complex128 accuracy in float-float arithmetic on the FP32 pipe (dtype c128f), same
+        # handle, same memory streams (16 B per complex, 8 B per value)
+        op.reserve("c128f", R, M)
+        device.cheb_moments(op, M, v, dtype="c128f")
+        torch.cuda.synchronize()
+        lib.kpm_ell_profile(op.handle, 1)
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(a.steps):
+            mu_f = device.cheb_moments(op, M, v, dtype="c128f")
+        f1.record(stream)
+        torch.cuda.synchronize()
+        _capi.check(lib.kpm_ell_profile_read(op.handle, ctypes.byref(loop_ms), ctypes.byref(launches),
+                                             ctypes.byref(rows)))
+        lib.kpm_ell_profile(op.handle, 0)
+        ms_f = max_over_ranks(f0.elapsed_time(f1), world) / a.steps
+        f_launch_s = (loop_ms.value * 1e-3) / max(1, launches.value)
+        f_gbs = bytes_per_launch / f_launch_s / 1e9
+        line["c128f"] = {
+            "value": float(n) * R * (M - 1) * world / (ms_f * 1e-3), "ms_per_step": ms_f,
+            "roofline": {"bound": "hbm", "achieved": f_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": f_gbs / hbm_peak,
+                         "kernel": "ff_next_kernel (float-float, bulk-copy staged, producer warp)",
+                         "avg_launch_ms": f_launch_s * 1e3},
+            "max_abs_diff_vs_c128_over_mu0": float(np.max(np.abs(mu_f.cpu().numpy() - mu_h))
+                                                   / np.max(np.abs(mu_h[:, 0]))),
+            "note": "dtype KPM_C128F: every real as a float pair (~48 bits), FP32 pipe; opt-in"}
     clocks = clk.summary()
     if clocks is not None:
         line["clocks"] = clocks

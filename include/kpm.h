@@ -49,6 +49,8 @@ extern "C" {
 /* ---- precision selectors ----------------------------------------------- */
 #define KPM_C128 0   /* complex128 recursion, FP64 moments (the drop-in form)   */
 #define KPM_C64 1    /* complex64 recursion and values, FP64 moment accumulation */
+#define KPM_C128F 2  /* complex128 accuracy in float-float arithmetic on the FP32 pipe
+                        (kpm_cheb_moments without mu_rr only; see there)           */
 
 /* ---- operator creation flags ------------------------------------------- */
 #define KPM_FLAG_DEVICE_PTRS 1u   /* data/indices are device pointers        */
@@ -128,6 +130,11 @@ int kpm_ell_dot(kpm_ell* h, double a_re, double a_im, double b_re, double b_im,
  */
 int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r,
                      const double* v_l, double* mu, double* mu_rr, void* stream);
+/* dtype KPM_C128F: the same moments with every real number carried as a pair of
+ * floats (~48 significant bits; exact products and sums), so the recursion runs on
+ * the FP32 pipe -- GB300's FP64 rate is 1/64 of its FP32 rate -- with the memory
+ * streams of complex128 (16 bytes per complex).  Within 1e-10 per order of the
+ * complex128 form.  No counterpart in the reference.  mu_rr must be NULL. */
 
 /*
  * out[r] = sum_{m<M} c[m] T_m(H) v[r]   (c: device [M] c128; v, out: device [R][n] c128;

@@ -25,12 +25,13 @@ KPM_ERR_TOO_LARGE = 10
 
 KPM_C128 = 0
 KPM_C64 = 1
+KPM_C128F = 2  # complex128 accuracy in float-float arithmetic (moments only)
 
 KPM_FLAG_DEVICE_PTRS = 1
 KPM_FLAG_SPLIT_DIAG = 2
 KPM_FLAG_DOUBLING = 4
 
-DTYPES = {"c128": KPM_C128, "complex128": KPM_C128, "c64": KPM_C64, "complex64": KPM_C64}
+DTYPES = {"c128": KPM_C128, "complex128": KPM_C128, "c64": KPM_C64, "complex64": KPM_C64, "c128f": KPM_C128F}
 
 # Every symbol include/kpm.h declares, with (restype, argtypes).
 _P = ctypes.c_void_p
@@ -137,10 +138,10 @@ def check(status: int, what: str = "") -> None:
 
 def dtype_code(dtype) -> int:
     if isinstance(dtype, int):
-        if dtype in (KPM_C128, KPM_C64):
+        if dtype in (KPM_C128, KPM_C64, KPM_C128F):
             return dtype
     elif str(dtype) in DTYPES:
         return DTYPES[str(dtype)]
     elif str(dtype).replace("torch.", "") in DTYPES:
         return DTYPES[str(dtype).replace("torch.", "")]
-    raise ValueError("unknown KPM dtype %r (use 'c128' or 'c64')" % (dtype,))
+    raise ValueError("unknown KPM dtype %r (use 'c128', 'c64' or 'c128f')" % (dtype,))

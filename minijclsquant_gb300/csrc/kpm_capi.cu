@@ -736,6 +736,17 @@ int kpm_ell_info(const kpm_ell* h, int64_t* n_rows, int* len_row, int* is_real, 
 
 int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M) {
   if (!h || R < 1 || M < 1) return KPM_ERR_INVALID_ARG;
+  if (dtype == KPM_C128F) {  // float-float: vectors of 16 B per complex, partials for any grid
+    KPM_TRY(ensure_f32_values(h, 0));
+    const int Rg = pow2_group(R);
+    const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+    KPM_TRY(ensure(h->ws.ta, vb));
+    KPM_TRY(ensure(h->ws.tb, vb));
+    KPM_TRY(ensure(h->ws.vl, vb));
+    KPM_TRY(ensure(h->ws.part, (size_t)kChunk * 6 * h->sm_count * Rg * sizeof(double2)));
+    KPM_CUDA_TRY(cudaDeviceSynchronize());
+    return KPM_OK;
+  }
   KPM_TRY(check_dtype(dtype));
   const bool f32 = dtype == KPM_C64;
   if (f32) KPM_TRY(ensure_f32_values(h, 0));
@@ -786,9 +797,18 @@ int kpm_ell_dot(kpm_ell* h, double a_re, double a_im, double b_re, double b_im, 
 int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r, const double* v_l, double* mu,
                      double* mu_rr, void* stream) {
   if (!h || !v_r || !mu || R < 1 || M < 1) return KPM_ERR_INVALID_ARG;
+  cudaStream_t s = as_stream(stream);
+  if (dtype == KPM_C128F) {  // float-float complex128, one moment set
+    if (mu_rr) return KPM_ERR_UNSUPPORTED;
+    for (int r0 = 0; r0 < R;) {
+      const int Rg = pow2_group(R - r0);
+      KPM_TRY(moments_group_ff(h, R, r0, Rg, M, v_r, v_l, mu, s));
+      r0 += Rg;
+    }
+    return KPM_OK;
+  }
   KPM_TRY(check_dtype(dtype));
   const bool f32 = dtype == KPM_C64;
-  cudaStream_t s = as_stream(stream);
   if (f32) KPM_TRY(ensure_f32_values(h, s));
   for (int r0 = 0; r0 < R;) {
     const int Rg = pow2_group(R - r0);

@@ -1,0 +1,497 @@
+// kpm_ff.cu -- complex128 Chebyshev moments in float-float arithmetic (KPM_C128F).
+//
+// GB300 issues FP64 fused multiply-adds at 1/64 of its FP32 rate, so the
+// complex128 recursion is bound by the FP64 pipe with HBM bandwidth to spare.
+// This form keeps complex128 accuracy with FP32 instructions: every real number is
+// an unevaluated pair hi + lo of floats (~48 significant bits), products are split
+// exactly (TwoProduct through FMA) and sums are exact (TwoSum), so one step
+//
+//   T_{m+1} = 2H T_m - T_{m-1},   moments <v_l | T_{m+1}>
+//
+// rounds only at the 2^-48 level.  A complex number is a float4 {re_hi, im_hi,
+// re_lo, im_lo}: 16 bytes, the size of a complex128, so the memory streams are
+// those of the complex128 kernels.  The operator values are the exact float pairs
+// of 2H that the complex64 path uses (hi = fl32(2h), lo = fl32(2h - hi)).
+// Moment products are accumulated as float pairs over at most kFlush rows per
+// thread and then in FP64.  (Float-float arithmetic: T. J. Dekker, Numer. Math. 18
+// (1971) 224; D. E. Knuth, TAOCP vol. 2, 4.2.2.)
+//
+// Kernels: the first step (T_1 = H T_0, mu_0, mu_1) grid-stride, the later steps
+// with the bulk-copy stages and producer warp of the staged step kernels.  Each
+// thread serves one complex of one vector (R threads per row).
+#include "kpm_ws.cuh"
+
+namespace kpm {
+
+namespace {
+
+constexpr int kFfFlush = 8;
+
+struct FF {  // complex value (rh + rl) + i (ih + il)
+  float rh, ih, rl, il;
+};
+
+__device__ __forceinline__ FF ff_of(const float4& q) { return FF{q.x, q.y, q.z, q.w}; }
+__device__ __forceinline__ float4 ff_raw(const FF& a) { return make_float4(a.rh, a.ih, a.rl, a.il); }
+
+// (hi, lo) += (ah + al)(bh + bl); the al*bl term (below 2^-48 relative) is dropped
+__device__ __forceinline__ void ff_madd(float& hi, float& lo, float ah, float al, float bh, float bl) {
+  two_prod_add(hi, lo, ah, bh);
+  lo = __fmaf_rn(ah, bl, lo);
+  lo = __fmaf_rn(al, bh, lo);
+}
+
+// (hi, lo) -> (s, e), s = fl(hi + lo), e the exact remainder
+__device__ __forceinline__ void ff_norm(float& hi, float& lo) {
+  const float s = __fadd_rn(hi, lo);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(lo, bp));
+  hi = s;
+  lo = e;
+}
+
+// acc += h x, h real (float2 {hi, lo}) or complex (float4 {re_hi, im_hi, re_lo, im_lo})
+__device__ __forceinline__ void ff_mac(FF& a, float2 h, const FF& x) {
+  ff_madd(a.rh, a.rl, h.x, h.y, x.rh, x.rl);
+  ff_madd(a.ih, a.il, h.x, h.y, x.ih, x.il);
+}
+__device__ __forceinline__ void ff_mac(FF& a, float4 h, const FF& x) {
+  ff_madd(a.rh, a.rl, h.x, h.z, x.rh, x.rl);
+  ff_madd(a.rh, a.rl, -h.y, -h.w, x.ih, x.il);
+  ff_madd(a.ih, a.il, h.x, h.z, x.ih, x.il);
+  ff_madd(a.ih, a.il, h.y, h.w, x.rh, x.rl);
+}
+
+// moment accumulator: (re, im) as float pairs, += conj(l) t
+struct FFMom {
+  float rh, rl, ih, il;
+};
+__device__ __forceinline__ void ff_cdot(FFMom& m, const FF& l, const FF& t) {
+  ff_madd(m.rh, m.rl, l.rh, l.rl, t.rh, t.rl);
+  ff_madd(m.rh, m.rl, l.ih, l.il, t.ih, t.il);
+  ff_madd(m.ih, m.il, l.rh, l.rl, t.ih, t.il);
+  ff_madd(m.ih, m.il, -l.ih, -l.il, t.rh, t.rl);
+}
+__device__ __forceinline__ void ff_fold(double& re, double& im, FFMom& m) {
+  re += (double)m.rh + (double)m.rl;
+  im += (double)m.ih + (double)m.il;
+  m = FFMom{0.f, 0.f, 0.f, 0.f};
+}
+
+template <bool REAL>
+struct FFVal { using type = float2; };
+template <>
+struct FFVal<false> { using type = float4; };
+
+// Grid-stride step.  FIRST: T_1 = (1/2)(2H) T_0 and the moments of T_0 and T_1,
+// partials [2 steps][grid][R].  NEXT (operators too wide for the staged stages):
+// T_{m+1} = 2H T_m - T_{m-1} in place and <v_l|T_{m+1}>, partials [grid][R].
+template <bool REAL, int R, bool NEXT>
+__global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
+  using MV = typename FFVal<REAL>::type;
+  constexpr int RPB = kBlock / R;
+  __shared__ double2 red[(kBlock / 32) * R];
+  const int sub = threadIdx.x % R, rl = threadIdx.x / R;
+  const MV* __restrict__ val = static_cast<const MV*>(p.val);
+  const float4* __restrict__ tcur = static_cast<const float4*>(p.tcur);
+  const float4* __restrict__ vl = static_cast<const float4*>(p.vl);
+  float4* tout = static_cast<float4*>(p.tout);
+  double zr[1] = {0.0}, zi[1] = {0.0}, mr[1] = {0.0}, mi[1] = {0.0};
+  FFMom z{0.f, 0.f, 0.f, 0.f}, m{0.f, 0.f, 0.f, 0.f};
+  int pending = 0;
+  for (int64_t row = (int64_t)blockIdx.x * RPB + rl; row < p.n_pad; row += (int64_t)gridDim.x * RPB) {
+    const int64_t vi = row * R + sub;
+    FF acc{0.f, 0.f, 0.f, 0.f};
+    if (NEXT) {
+      const FF o = ff_of(tout[vi]);
+      acc = FF{-o.rh, -o.ih, -o.rl, -o.il};
+    }
+    for (int s = 0; s < p.L; ++s) {
+      const int32_t c = __ldcs(p.col + (int64_t)s * p.ld + row);
+      const MV h = __ldcs(val + (int64_t)s * p.ld + row);
+      ff_mac(acc, h, ff_of(__ldg(tcur + (int64_t)c * R + sub)));
+    }
+    ff_norm(acc.rh, acc.rl);
+    ff_norm(acc.ih, acc.il);
+    if (!NEXT) acc = FF{0.5f * acc.rh, 0.5f * acc.ih, 0.5f * acc.rl, 0.5f * acc.il};  // exact
+    tout[vi] = ff_raw(acc);
+    const FF l = ff_of(__ldg(vl + vi));
+    if (!NEXT) ff_cdot(z, l, ff_of(__ldg(tcur + vi)));
+    ff_cdot(m, l, acc);
+    if (++pending == kFfFlush) {
+      pending = 0;
+      ff_fold(zr[0], zi[0], z);
+      ff_fold(mr[0], mi[0], m);
+    }
+  }
+  ff_fold(zr[0], zi[0], z);
+  ff_fold(mr[0], mi[0], m);
+  if (NEXT) {
+    block_reduce_store<R, 1>(mr, mi, p.part + (int64_t)blockIdx.x * R, red);
+  } else {
+    block_reduce_store<R, 1>(zr, zi, p.part + (int64_t)blockIdx.x * R, red);
+    block_reduce_store<R, 1>(mr, mi, p.part + p.part_step_stride + (int64_t)blockIdx.x * R, red);
+  }
+}
+
+// T_{m+1} = 2H T_m - T_{m-1} (in place over T_{m-1}) and <v_l|T_{m+1}> per CTA, with
+// the staged tiles, producer warp and full/empty barriers of cheb_next_ws_kernel.
+template <bool REAL, int R, int U>
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) ff_next_kernel(const StepParams p) {
+  using MV = typename FFVal<REAL>::type;
+  constexpr int RPB = kBlock / R;
+  constexpr int TILE = RPB * U;
+  constexpr int kWarps = kBlock / 32;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[kWsStages];
+  __shared__ __align__(8) uint64_t empty[kWsStages];
+  __shared__ double2 red[kWarps * R];
+
+  const int L = p.L;
+  const uint32_t col_b = (uint32_t)align16((size_t)L * TILE * 4);
+  const uint32_t val_b = (uint32_t)align16((size_t)L * TILE * sizeof(MV));
+  const uint32_t vec_b = (uint32_t)(TILE * R * sizeof(float4));
+  const uint32_t stage_b = col_b + val_b + 2 * vec_b;
+  const int ntiles = (int)(p.n_pad / TILE);
+  const int my_count = ((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  auto tile_of = [&](int k) -> int64_t { return (int64_t)blockIdx.x + (int64_t)k * gridDim.x; };
+
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int s = 0; s < kWsStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kWarps);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == kWarps) {  // producer
+    if (lane == 0 && my_count > 0) {
+      TileCopy tc;
+      const uint64_t pol = l2_evict_first_policy();
+      tc.col = p.col;
+      tc.val = static_cast<const unsigned char*>(p.val);
+      tc.old = static_cast<const unsigned char*>(p.tout);
+      tc.vl = static_cast<const unsigned char*>(p.vl);
+      tc.vl2 = nullptr;
+      tc.ld = p.ld;
+      tc.L = L;
+      tc.col_slab = TILE * 4;
+      tc.val_slab = (uint32_t)(TILE * sizeof(MV));
+      tc.vec_slab = vec_b;
+      tc.vl_slab = vec_b;
+      tc.col_b = col_b;
+      tc.val_b = val_b;
+      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + 2 * vec_b;
+      int issued = 0;
+      for (int k = 0; k < my_count; ++k) {
+        const int st = k % kWsStages;
+        if (k >= kWsStages && !mbar_wait_bounded(&empty[st], (uint32_t)(((k / kWsStages) - 1) & 1))) {
+          atomicExch(p.err, KPM_ERR_TIMEOUT);
+          break;
+        }
+        fence_proxy_async_shared();
+        issue_tile(tc, smem + st * stage_b, &full[st], tile_of(k) * TILE, R * (int)sizeof(float4), pol);
+        issued = k + 1;
+      }
+      for (int q = issued > kWsStages ? issued - kWsStages : 0; q < issued; ++q)
+        (void)mbar_wait_bounded(&full[q % kWsStages], (uint32_t)((q / kWsStages) & 1));
+    }
+    return;
+  }
+
+  const float4* __restrict__ tcur = static_cast<const float4*>(p.tcur);
+  float4* tout = static_cast<float4*>(p.tout);
+  const int sub = threadIdx.x % R, rl = threadIdx.x / R;
+  double mr[1] = {0.0}, mi[1] = {0.0};
+  FFMom mom{0.f, 0.f, 0.f, 0.f};
+  int pending = 0;
+  bool dead = false;
+  for (int k = 0; k < my_count; ++k) {
+    const int st = k % kWsStages;
+    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / kWsStages) & 1));
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok && !dead) {
+      if (lane == 0) atomicExch(p.err, KPM_ERR_TIMEOUT);
+      dead = true;
+    }
+    if (!ok) continue;
+    const unsigned char* base = smem + st * stage_b;
+    const int32_t* scol = reinterpret_cast<const int32_t*>(base);
+    const MV* sval = reinterpret_cast<const MV*>(base + col_b);
+    const float4* sold = reinterpret_cast<const float4*>(base + col_b + val_b);
+    const float4* svl = reinterpret_cast<const float4*>(base + col_b + val_b + vec_b);
+    const int64_t row0 = tile_of(k) * TILE;
+    FF acc[U], l[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const FF o = ff_of(sold[(u * RPB + rl) * R + sub]);
+      acc[u] = FF{-o.rh, -o.ih, -o.rl, -o.il};
+    }
+    for (int s = 0; s < L; s += 4) {
+      int c[U][4];
+      MV h[U][4];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (s + j < L) {
+            c[u][j] = scol[(s + j) * TILE + u * RPB + rl];
+            h[u][j] = sval[(s + j) * TILE + u * RPB + rl];
+          }
+      float4 x[U][4];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (s + j < L) x[u][j] = __ldg(tcur + (int64_t)c[u][j] * R + sub);
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          if (s + j < L) ff_mac(acc[u], h[u][j], ff_of(x[u][j]));
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      ff_norm(acc[u].rh, acc[u].rl);
+      ff_norm(acc[u].ih, acc[u].il);
+      l[u] = ff_of(svl[(u * RPB + rl) * R + sub]);
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      tout[(row0 + u * RPB + rl) * R + sub] = ff_raw(acc[u]);
+      ff_cdot(mom, l[u], acc[u]);
+      if (++pending == kFfFlush) {
+        pending = 0;
+        ff_fold(mr[0], mi[0], mom);
+      }
+    }
+  }
+  ff_fold(mr[0], mi[0], mom);
+  block_reduce_store<R, 1>(mr, mi, p.part + (int64_t)blockIdx.x * R, red, true);
+}
+
+// complex128 [R][n] (vector-major) -> float pairs [n_pad][Rg] for vectors r0 .. r0 + Rg
+__global__ void ff_pack_kernel(const double2* __restrict__ src, int64_t n, int64_t n_pad, int R, int r0, int Rg,
+                               float4* __restrict__ dst) {
+  const int64_t total = n_pad * Rg;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t / Rg;
+    const int r = (int)(t % Rg);
+    double2 z = make_double2(0.0, 0.0);
+    if (row < n) z = src[(int64_t)(r0 + r) * n + row];
+    const float xh = (float)z.x, yh = (float)z.y;
+    dst[t] = make_float4(xh, yh, (float)(z.x - (double)xh), (float)(z.y - (double)yh));
+  }
+}
+
+template <bool REAL, int R, int U>
+bool ff_smem_attr(size_t smem) {
+  static size_t configured = 0;
+  if (smem <= configured) return true;
+  if (cudaFuncSetAttribute(ff_next_kernel<REAL, R, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  configured = smem;
+  return true;
+}
+
+template <bool REAL, int R, int U>
+size_t ff_stage_bytes(int L) {
+  constexpr int TILE = (kBlock / R) * U;
+  return align16((size_t)L * TILE * 4) + align16((size_t)L * TILE * sizeof(typename FFVal<REAL>::type)) +
+         2 * (size_t)TILE * R * sizeof(float4);
+}
+
+// One launch: kind -1 the first step, 0 a grid-stride later step, 1 / 2 a staged
+// later step with U = kind rows per thread.
+template <bool REAL, int R, int U>
+int ff_launch_staged(const StepParams& p, int grid, cudaStream_t s) {
+  const size_t smem = kWsStages * ff_stage_bytes<REAL, R, U>(p.L);
+  if (!ff_smem_attr<REAL, R, U>(smem)) return KPM_ERR_UNSUPPORTED;
+  ff_next_kernel<REAL, R, U><<<grid, kWsThreads, smem, s>>>(p);
+  return check_cuda(cudaGetLastError());
+}
+
+template <bool REAL, int R>
+int ff_launch(int kind, const StepParams& p, int grid, cudaStream_t s) {
+  if (kind < 0)
+    ff_step_kernel<REAL, R, false><<<grid, kBlock, 0, s>>>(p);
+  else if (kind == 0)
+    ff_step_kernel<REAL, R, true><<<grid, kBlock, 0, s>>>(p);
+  else
+    return kind == 2 ? ff_launch_staged<REAL, R, 2>(p, grid, s) : ff_launch_staged<REAL, R, 1>(p, grid, s);
+  return check_cuda(cudaGetLastError());
+}
+
+template <bool REAL, int R, int U>
+int ff_ctas(int L) {
+  const size_t smem = kWsStages * ff_stage_bytes<REAL, R, U>(L);
+  if (smem > 200 * 1024 || !ff_smem_attr<REAL, R, U>(smem)) return 0;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ff_next_kernel<REAL, R, U>, kWsThreads, smem) !=
+      cudaSuccess) {
+    (void)cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int ff_dispatch(bool real, int R, int kind, const StepParams& p, int grid, cudaStream_t s) {
+#define KPM_FF(RR) \
+  return real ? ff_launch<true, RR>(kind, p, grid, s) : ff_launch<false, RR>(kind, p, grid, s)
+  switch (R) {
+    case 1: KPM_FF(1);
+    case 2: KPM_FF(2);
+    case 4: KPM_FF(4);
+    case 8: KPM_FF(8);
+    default: return KPM_ERR_UNSUPPORTED;
+  }
+#undef KPM_FF
+}
+
+int ff_occupancy(bool real, int R, int U, int L) {
+#define KPM_FO(RR) \
+  return U == 2 ? (real ? ff_ctas<true, RR, 2>(L) : ff_ctas<false, RR, 2>(L)) \
+                : (real ? ff_ctas<true, RR, 1>(L) : ff_ctas<false, RR, 1>(L))
+  switch (R) {
+    case 1: KPM_FO(1);
+    case 2: KPM_FO(2);
+    case 4: KPM_FO(4);
+    case 8: KPM_FO(8);
+    default: return 0;
+  }
+#undef KPM_FO
+}
+
+// The later-step kernel for (operator, R): the grid-stride kernel or the staged
+// kernel with 1 or 2 rows per thread, timed on the operator (a few launches on
+// zeroed vectors) and kept in the handle's tuned list (key 2000 + 10 R).
+int ff_config(kpm_ell_s* h, int Rg, cudaStream_t s, StepConfig* out) {
+  const int key = 2000 + Rg * 10;
+  for (auto& kv : h->tuned)
+    if (kv.first == key) {
+      *out = kv.second;
+      return KPM_OK;
+    }
+  std::vector<StepConfig> cands;
+  StepConfig c0;
+  c0.kind = 0;
+  c0.grid = grid_for(h, Rg, 1);
+  cands.push_back(c0);
+  for (int U = 1; U <= 2; ++U) {
+    const int occ = ff_occupancy(h->is_real != 0, Rg, U, h->L);
+    if (occ <= 0) continue;
+    const int64_t ntiles = h->n_pad / ((kBlock / Rg) * U);
+    StepConfig c;
+    c.kind = 2;
+    c.U = U;
+    c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
+    cands.push_back(c);
+  }
+  if (cands.size() > 1) {
+    int max_grid = 0;
+    for (auto& c : cands) max_grid = std::max(max_grid, c.grid);
+    const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+    Workspace& ws = h->ws;
+    KPM_TRY(ensure(ws.ta, vb));
+    KPM_TRY(ensure(ws.tb, vb));
+    KPM_TRY(ensure(ws.vl, vb));
+    KPM_TRY(ensure(ws.part, (size_t)max_grid * Rg * sizeof(double2)));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.ta.p, 0, vb, s));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.tb.p, 0, vb, s));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.vl.p, 0, vb, s));
+    StepParams p = base_params(h, true);
+    p.tcur = ws.ta.p;
+    p.tout = ws.tb.p;
+    p.vl = ws.vl.p;
+    p.part = static_cast<double2*>(ws.part.p);
+    cudaEvent_t e0, e1;
+    KPM_CUDA_TRY(cudaEventCreate(&e0));
+    KPM_CUDA_TRY(cudaEventCreate(&e1));
+    for (auto& c : cands) {
+      const int kind = c.kind == 0 ? 0 : c.U;
+      KPM_TRY(ff_dispatch(h->is_real != 0, Rg, kind, p, c.grid, s));
+      KPM_CUDA_TRY(cudaEventRecord(e0, s));
+      for (int r = 0; r < 3; ++r) KPM_TRY(ff_dispatch(h->is_real != 0, Rg, kind, p, c.grid, s));
+      KPM_CUDA_TRY(cudaEventRecord(e1, s));
+      KPM_CUDA_TRY(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      KPM_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+      c.us = 1e3f * ms / 3;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
+  StepConfig best = cands[0];
+  for (auto& c : cands)
+    if (c.us < best.us) best = c;
+  h->tuned.emplace_back(key, best);
+  *out = best;
+  return KPM_OK;
+}
+
+}  // namespace
+
+// DOS / two-vector moments <v_l|T_m v_r> of one group of Rg vectors in float-float arithmetic.
+int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v_r, const double* v_l, double* mu,
+                     cudaStream_t s) {
+  KPM_TRY(ensure_f32_values(h, s));
+  const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  StepConfig cfg;
+  KPM_TRY(ff_config(h, Rg, s, &cfg));
+  const int grid_first = grid_for(h, Rg, 1);
+  const int grid_next = cfg.grid;
+  const int grid = std::max(grid_next, grid_first);
+  const int64_t step_stride = (int64_t)grid * Rg;
+  KPM_TRY(ensure(ws.part, (size_t)kChunk * step_stride * sizeof(double2)));
+  const int64_t total = h->n_pad * Rg;
+  const int pg = (int)std::min<int64_t>((total + 255) / 256, 65536);
+  ff_pack_kernel<<<pg, 256, 0, s>>>(reinterpret_cast<const double2*>(v_r), h->n, h->n_pad, R, r0, Rg,
+                                    static_cast<float4*>(ws.ta.p));
+  ff_pack_kernel<<<pg, 256, 0, s>>>(reinterpret_cast<const double2*>(v_l ? v_l : v_r), h->n, h->n_pad, R, r0, Rg,
+                                    static_cast<float4*>(ws.vl.p));
+  KPM_CUDA_TRY(cudaGetLastError());
+  double2* part = static_cast<double2*>(ws.part.p);
+  double* outs[2] = {mu, mu};
+  StepParams p = base_params(h, true);  // the float-pair values
+  p.vl = ws.vl.p;
+  p.part_step_stride = (int64_t)grid_first * Rg;
+  p.tcur = ws.ta.p;
+  p.tout = ws.tb.p;
+  p.part = part;
+  KPM_TRY(ff_dispatch(h->is_real != 0, Rg, -1, p, grid_first, s));
+  KPM_TRY(reduce_partials(part, std::min(M, 2), 1, grid_first, Rg, outs, R, r0, M, 0, s));
+  void* tprev = ws.ta.p;
+  void* tcur = ws.tb.p;
+  int m0 = 2;
+  cudaEvent_t ev = nullptr;
+  if (M > 2) KPM_TRY(prof_begin(h, s, &ev));
+  for (int m = 2; m < M; ++m) {
+    if (m - m0 == kChunk) {
+      KPM_TRY(reduce_partials(part, kChunk, 1, grid_next, Rg, outs, R, r0, M, m0, s));
+      m0 = m;
+    }
+    p.tcur = tcur;
+    p.tout = tprev;
+    p.part = part + (int64_t)(m - m0) * grid_next * Rg;
+    KPM_TRY(ff_dispatch(h->is_real != 0, Rg, cfg.kind == 0 ? 0 : cfg.U, p, grid_next, s));
+    std::swap(tprev, tcur);
+  }
+  if (M > 2) KPM_TRY(prof_end(h, s, ev, M - 2));
+  if (M > m0) KPM_TRY(reduce_partials(part, M - m0, 1, grid_next, Rg, outs, R, r0, M, m0, s));
+  return KPM_OK;
+}
+
+}  // namespace kpm

@@ -181,6 +181,9 @@ int mu1_exact(const kpm_ell_s* h, const void* packed_f32, int Rg, const int64_t*
 int assemble_doubled(const double2* red_b, const double2* red_d, const double* corr, int rows, int K, int M,
                      double2* mu, int64_t mu_row_stride, int64_t mu_row0, cudaStream_t s);
 int check_dtype(int dtype);
+// KPM_C128F: moments of one vector group in float-float arithmetic (kpm_ff.cu).
+int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v_r, const double* v_l, double* mu,
+                     cudaStream_t s);
 
 // Rows per tile of the staged kernel (complex64 packs two vectors per thread).
 inline int staged_tile_rows(bool f32, int R, int U) {

@@ -50,6 +50,15 @@ __device__ __forceinline__ void ff_norm(float& hi, float& lo) {
   lo = e;
 }
 
+// (hi, lo) += (hi2, lo2), exact in the hi parts (TwoSum)
+__device__ __forceinline__ void ff_add(float& hi, float& lo, float hi2, float lo2) {
+  const float s = __fadd_rn(hi, hi2);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(hi2, bp));
+  hi = s;
+  lo = __fadd_rn(__fadd_rn(lo, lo2), e);
+}
+
 // acc += h x, h real (float2 {hi, lo}) or complex (float4 {re_hi, im_hi, re_lo, im_lo})
 __device__ __forceinline__ void ff_mac(FF& a, float2 h, const FF& x) {
   ff_madd(a.rh, a.rl, h.x, h.y, x.rh, x.rl);
@@ -137,7 +146,7 @@ __global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
 // T_{m+1} = 2H T_m - T_{m-1} (in place over T_{m-1}) and <v_l|T_{m+1}> per CTA, with
 // the staged tiles, producer warp and full/empty barriers of cheb_next_ws_kernel.
 template <bool REAL, int R, int U>
-__global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) ff_next_kernel(const StepParams p) {
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? 3 : 1)) ff_next_kernel(const StepParams p) {
   using MV = typename FFVal<REAL>::type;
   constexpr int RPB = kBlock / R;
   constexpr int TILE = RPB * U;
@@ -225,11 +234,13 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) ff_next_kernel(c
     const float4* sold = reinterpret_cast<const float4*>(base + col_b + val_b);
     const float4* svl = reinterpret_cast<const float4*>(base + col_b + val_b + vec_b);
     const int64_t row0 = tile_of(k) * TILE;
-    FF acc[U], l[U];
+    // even slots into acc, odd slots into acc2: two independent chains per component
+    FF acc[U], acc2[U], l[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       const FF o = ff_of(sold[(u * RPB + rl) * R + sub]);
       acc[u] = FF{-o.rh, -o.ih, -o.rl, -o.il};
+      acc2[u] = FF{0.f, 0.f, 0.f, 0.f};
     }
     for (int s = 0; s < L; s += 4) {
       int c[U][4];
@@ -252,10 +263,12 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) ff_next_kernel(c
       for (int u = 0; u < U; ++u)
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (s + j < L) ff_mac(acc[u], h[u][j], ff_of(x[u][j]));
+          if (s + j < L) ff_mac((j & 1) ? acc2[u] : acc[u], h[u][j], ff_of(x[u][j]));
     }
 #pragma unroll
     for (int u = 0; u < U; ++u) {
+      ff_add(acc[u].rh, acc[u].rl, acc2[u].rh, acc2[u].rl);
+      ff_add(acc[u].ih, acc[u].il, acc2[u].ih, acc2[u].il);
       ff_norm(acc[u].rh, acc[u].rl);
       ff_norm(acc[u].ih, acc[u].il);
       l[u] = ff_of(svl[(u * RPB + rl) * R + sub]);

@@ -442,9 +442,15 @@ def run_adjoint(a, steps, warmup):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / k
 
+    from minijclsquant_gb300 import _capi
+
     t_f = timeit(fwd, steps)
-    t_fb = timeit(fwd_bwd, steps)
+    t_fb = timeit(fwd_bwd, steps)  # float-float backward (the plan's default)
     go, gh = onsite.grad.detach().cpu().numpy(), hop.grad.detach().cpu().numpy()
+    plan.backward_dtype = _capi.KPM_C128  # the same pass in FP64 arithmetic
+    t_fb64 = timeit(fwd_bwd, steps)
+    go64, gh64 = onsite.grad.detach().cpu().numpy(), hop.grad.detach().cpu().numpy()
+    plan.backward_dtype = _capi.KPM_C128F
     pick = np.random.default_rng(7)
     half = a.adj_fd // 2
     params = [("onsite", int(i)) for i in pick.choice(n, half, replace=False)] + \
@@ -468,6 +474,11 @@ def run_adjoint(a, steps, warmup):
                         % (cells, cells, n, M, R),
             "forward_ms": 1e3 * t_f, "forward_backward_ms": 1e3 * t_fb, "backward_over_forward": (t_fb - t_f) / t_f,
             "fwd_plus_bwd_over_fwd": t_fb / t_f,
+            "backward": "float-float (KPM_C128F) adjoint, recompute and gradient; FP64 forward and checkpoints",
+            "fp64_backward": {"forward_backward_ms": 1e3 * t_fb64, "fwd_plus_bwd_over_fwd": t_fb64 / t_f,
+                              "max_abs_diff_vs_float_float_over_max_grad": float(
+                                  max(np.max(np.abs(go - go64)), np.max(np.abs(gh - gh64)))
+                                  / max(np.max(np.abs(go64)), np.max(np.abs(gh64))))},
             "fd_check": {"params": len(params), "h": h, "max_abs_err_over_max_grad": worst}}
 
 

@@ -182,6 +182,11 @@ int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const
 int kpm_ell_set_values(kpm_ell* h, const double* data, unsigned flags, void* stream);
 int kpm_adjoint_forward(kpm_ell* h, int R, int M, int ckpt, const double* v, double* mu, void* stream);
 int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream);
+/* kpm_adjoint_backward with the arithmetic chosen: KPM_C128 (FP64, as above) or
+ * KPM_C128F (the adjoint recursion, segment recompute and gradient in float-float
+ * arithmetic on the FP32 pipe; checkpoints and the result stay FP64; ~1e-14
+ * relative to the FP64 gradient). */
+int kpm_adjoint_backward_ex(kpm_ell* h, const double* c, double* grad, int dtype, void* stream);
 
 /* ---- Kubo-Greenwood moment matrix on the tensor cores ---------------------
  * No counterpart in the reference (its conductivity is the time-domain

@@ -70,6 +70,7 @@ SIGNATURES = {
     "kpm_batch_moments": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "kpm_ell_props": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "kpm_ell_set_doubling": (_I, [_P, _I]),
+    "kpm_adjoint_backward_ex": (_I, [_P, _P, _P, _I, _P]),
     "kpm_batch_props": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "kpm_batch_set_doubling": (_I, [_P, _I]),
     "kpm_batch_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),

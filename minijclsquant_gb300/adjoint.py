@@ -15,8 +15,9 @@ Jackson-damped DOS averaged over the vectors,
 
     rho(E) = (1/R) sum_r Re sum_m delta_m(E/a) g_m mu_m^(r)        (FP64);
 
-backward maps dL/drho to c_m, runs ``kpm_adjoint_backward`` and folds the
-per-slot derivatives into on-site and bond gradients (divided by a).
+backward maps dL/drho to c_m, runs the adjoint recursion (``kpm_adjoint_backward_ex``,
+float-float arithmetic by default) and folds the per-slot derivatives into on-site
+and bond gradients (divided by a).
 
 The reference has no derivatives; the forward quantity is its kpm_dos
 (jclsquant/observables.py:26-54) on these parameters.
@@ -37,7 +38,10 @@ from .observables import random_vector_generator
 
 class DosPlan:
     def __init__(self, nx, ny, M, R=4, n_energies=512, ckpt=32, onsite0=None, hopping0=None, t=-2.7,
-                 vector_seed=1000, bounds_factor=1.01, energy_margin=1e-3):
+                 vector_seed=1000, bounds_factor=1.01, energy_margin=1e-3, backward="c128f"):
+        """backward: arithmetic of the adjoint pass, "c128" (FP64) or "c128f" (float-float on
+        the FP32 pipe, ~1e-14 of the FP64 gradient); the forward is always FP64."""
+        self.backward_dtype = _capi.dtype_code(backward)
         arr = lattice.honeycomb_arrays(nx, ny, t=t, W=0.0, onsite=np.zeros(2 * nx * ny), with_geometry=False)
         self.n = arr["n"]
         self.L = arr["len_row"]
@@ -122,8 +126,8 @@ class _KPMDos(torch.autograd.Function):
         c = (plan.table.t() @ grad_rho.to(torch.float64)) / plan.R
         c = c.contiguous()
         g = torch.empty(plan.n * plan.L, dtype=torch.float64, device=grad_rho.device)
-        _capi.check(lib.kpm_adjoint_backward(plan.op.handle, c.data_ptr(), g.data_ptr(), stream),
-                    "kpm_adjoint_backward")
+        _capi.check(lib.kpm_adjoint_backward_ex(plan.op.handle, c.data_ptr(), g.data_ptr(), plan.backward_dtype,
+                                                stream), "kpm_adjoint_backward_ex")
         g = g / plan.a
         g_onsite = torch.zeros(plan.n, dtype=torch.float64, device=g.device)
         g_onsite.index_add_(0, plan.d_diag_site, g[plan.d_diag_slot])

@@ -3,7 +3,8 @@ gradient (which is itself checked against finite differences on the CPU), and
 the autograd DOS loss against central finite differences of the GPU forward.
 
 Tolerances: per-slot gradient vs oracle <= 1e-10 * max|grad|; autograd vs
-central differences (h = 1e-6) <= 1e-6 * max(|grad|) + 1e-8.
+central differences (h = 1e-6) <= 1e-6 * max(|grad|) + 1e-8.  Both backward
+arithmetics are held to them: FP64 and float-float (KPM_C128F).
 """
 import ctypes
 
@@ -25,8 +26,11 @@ def _problem(nx=6, ny=5, W=0.8, seed=3):
     return arr, arr["data"] / b[1]
 
 
+@pytest.mark.parametrize("backward", ["c128", "c128f"])
 @pytest.mark.parametrize("M,ckpt,R", [(2, 2, 1), (3, 2, 2), (50, 7, 4), (64, 32, 4), (40, 64, 8), (97, 3, 2)])
-def test_adjoint_gradient_matches_oracle(cuda_lib, M, ckpt, R):
+def test_adjoint_gradient_matches_oracle(cuda_lib, M, ckpt, R, backward):
+    from minijclsquant_gb300 import _capi
+
     import torch
 
     arr, d = _problem()
@@ -42,7 +46,8 @@ def test_adjoint_gradient_matches_oracle(cuda_lib, M, ckpt, R):
     assert cuda_lib.kpm_adjoint_forward(op.handle, R, M, ckpt, tv.data_ptr(), mu.data_ptr(), None) == 0
     tc = torch.from_numpy(c).cuda()
     g = torch.empty(n * L, dtype=torch.float64, device="cuda")
-    assert cuda_lib.kpm_adjoint_backward(op.handle, tc.data_ptr(), g.data_ptr(), None) == 0
+    assert cuda_lib.kpm_adjoint_backward_ex(op.handle, tc.data_ptr(), g.data_ptr(), _capi.dtype_code(backward),
+                                            None) == 0
     assert cuda_lib.kpm_ell_check(op.handle, None) == 0
     g = g.cpu().numpy()
     ref = sum(oracle.adjoint_grad(M, d, arr["indices"], L, vs[r], c) for r in range(R))
@@ -52,7 +57,8 @@ def test_adjoint_gradient_matches_oracle(cuda_lib, M, ckpt, R):
                                           oracle.rec_A_tab(M, d, arr["indices"], L, vs[r]), 1e-10)[0]
 
 
-def test_autograd_dos_loss_matches_finite_differences(cuda_lib):
+@pytest.mark.parametrize("backward", ["c128", "c128f"])
+def test_autograd_dos_loss_matches_finite_differences(cuda_lib, backward):
     import torch
 
     from minijclsquant_gb300 import adjoint
@@ -61,7 +67,8 @@ def test_autograd_dos_loss_matches_finite_differences(cuda_lib):
     nx, ny = 8, 7
     n = 2 * nx * ny
     plan0 = adjoint.DosPlan(nx, ny, M=96, R=2, n_energies=64, ckpt=8,
-                            onsite0=rng.uniform(-0.5, 0.5, n), hopping0=-2.7 + rng.uniform(-0.1, 0.1, 3 * nx * ny))
+                            onsite0=rng.uniform(-0.5, 0.5, n), hopping0=-2.7 + rng.uniform(-0.1, 0.1, 3 * nx * ny),
+                            backward=backward)
     onsite = torch.tensor(rng.uniform(-0.5, 0.5, n), dtype=torch.float64, device="cuda", requires_grad=True)
     hop = torch.tensor(-2.7 + rng.uniform(-0.1, 0.1, plan0.n_bonds), dtype=torch.float64, device="cuda",
                        requires_grad=True)

@@ -64,6 +64,10 @@ def parse():
     ap.add_argument("--adj-cells", type=int, default=512)
     ap.add_argument("--adj-M", type=int, default=1024)
     ap.add_argument("--adj-fd", type=int, default=64, help="parameters checked by central differences")
+    ap.add_argument("--no-time", action="store_true", help="skip the time-evolution (for_time) measurement")
+    ap.add_argument("--time-M", type=int, default=64, help="series terms per time step")
+    ap.add_argument("--time-len", type=int, default=8, help="time steps per timed step")
+    ap.add_argument("--time-dt", type=float, default=16.0, help="time step in units of 1/a (scaled H)")
     ap.add_argument("--no-kubo", action="store_true", help="skip the Kubo-Greenwood mu_nm measurement")
     ap.add_argument("--kubo-cells", type=int, default=1024)
     ap.add_argument("--kubo-Nm", type=int, default=256)
@@ -198,6 +202,100 @@ def cpu_rec_A_tab(M, prob, v, threads):
     t0 = time.perf_counter()
     oracle.rec_A_tab(M, prob["data_kpm"], prob["indices"], L, v, threads=threads)
     return time.perf_counter() - t0, "port"
+
+
+def cpu_time_evolve(M2, prob, vs, threads):
+    """One time step of U and U_c on the CPU: the loop of jclsquant/recurrence_functions.py:114-143
+    (aAxby + axpy2 per order) over jclsquant's own kernels, else the oracle.  (seconds, kind)."""
+    from minijclsquant_gb300.kernel_and_moments import moments_U
+
+    blas = cpu_reference_kernels()
+    n, L = prob["n"], prob["L"]
+    c = moments_U(1.0, M2).astype(np.complex128)
+    if blas is not None:
+        data, idx = prob["data_kpm"], prob["indices"]
+        t0 = time.perf_counter()
+        for v in vs:
+            T0 = np.copy(v)
+            T1 = np.zeros(n, dtype=np.complex128)
+            blas.aAxby(1 + 0j, 0 + 0j, v, T1, data, idx, L, n, threads)
+            acc = c[0] * v
+            acc += c[1] * T1
+            for m in range(2, M2):
+                blas.aAxby(2.0 + 0j, -1 + 0j, T1, T0, data, idx, L, n, threads)
+                T0, T1 = T1, T0
+                blas.axpy2(c[m], 1 + 0j, T1, acc, n, threads)
+        return time.perf_counter() - t0, "reference"
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    for v in vs:
+        oracle.rec_A_vec(M2, prob["data_kpm"], prob["indices"], L, c, v, threads=threads)
+    return time.perf_counter() - t0, "port"
+
+
+def run_time_evolution(a, op, n, L, prob, hbm_peak, world):
+    """for_time (obv.cu:93-122) on the DOS lattice: U and U_c, one group of two vectors,
+    advanced len_t times by the series of exp(-i H dt) with M2 terms.  Value: site-steps/s,
+    N * 2 * (M2 - 1) * len_t per timed step.  The dominant kernel is the series step:
+    T_{m+1} = 2H T_m - T_{m-1} and series += c_m T_{m+1}, algorithmic bytes per row
+    L (value + index) + 2 vectors x 5 x 16 B (T_m gathered once, T_{m-1} read, T_{m+1}
+    written, the series read and written)."""
+    import ctypes
+
+    import torch
+
+    from minijclsquant_gb300 import _capi, device
+    from minijclsquant_gb300.kernel_and_moments import moments_U
+
+    lib = _capi.lib()
+    stream = torch.cuda.current_stream()
+    M2, len_t, R2 = a.time_M, a.time_len, 2
+    c = torch.from_numpy(moments_U(a.time_dt, M2).astype(np.complex128)).cuda()
+    uv = torch.from_numpy(random_vectors(n, R2, 4242)).cuda()
+    for _ in range(max(1, a.warmup)):
+        out = device.time_evolve(op, M2, c, 1, uv)  # the first call also tunes the series step
+    torch.cuda.synchronize()
+    loop_ms, launches, rows = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    lib.kpm_ell_profile(op.handle, 1)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        out = device.time_evolve(op, M2, c, len_t, uv)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    _capi.check(lib.kpm_ell_profile_read(op.handle, ctypes.byref(loop_ms), ctypes.byref(launches),
+                                         ctypes.byref(rows)))
+    lib.kpm_ell_profile(op.handle, 0)
+    ms = max_over_ranks(e0.elapsed_time(e1), world) / a.steps
+    n0 = torch.linalg.vector_norm(uv, dim=1)
+    drift = float(torch.max(torch.abs(torch.linalg.vector_norm(out, dim=1) - n0) / n0))
+    val_bytes = 8 if op.is_real else 16
+    bytes_per_row = L * (val_bytes + 4) + R2 * 5 * 16
+    step_s = loop_ms.value * 1e-3 / max(1, launches.value)
+    gbs = float(n) * bytes_per_row / step_s / 1e9
+    kind, rpt, grid, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+    _capi.check(lib.kpm_ell_series_config(op.handle, _capi.KPM_C128, R2, ctypes.byref(kind), ctypes.byref(rpt),
+                                          ctypes.byref(grid), ctypes.byref(us)))
+    kname = ("cheb_next_ws_kernel<SER> (producer warp, %d row(s)/thread)" % rpt.value if kind.value == 2
+             else "cheb_step_kernel (grid-stride, MODE_NEXT STORE|SERIES)")
+    blk = {"value": float(n) * R2 * (M2 - 1) * len_t * world / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+           "config": {"vectors": "U, U_c", "M2": M2, "len_t": len_t, "dt": a.time_dt, "sites": n},
+           "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                        "kernel": kname, "grid": grid.value, "algorithmic_bytes_per_launch": float(n) * bytes_per_row,
+                        "avg_launch_ms": step_s * 1e3},
+           "norm_drift": drift,
+           "gpu_launches": len_t * (M2 + 1) * a.steps,
+           "note": "exp(-i H dt) by its Chebyshev series (moments_U); norm_drift = max |(|U(t)| - |U(0)|)| / |U(0)|"}
+    if not a.no_cpu and world == 1:
+        threads = os.cpu_count() or 1
+        vs = random_vectors(n, R2, 4242)
+        dt, kind_s = cpu_time_evolve(M2, prob, vs, threads)
+        blk["cpu_baseline"] = {"value": float(n) * R2 * (M2 - 1) / dt, "unit": UNIT, "cores": threads,
+                               "kind": kind_s, "sample": "one time step of U and U_c (M2=%d) on the full %d-site "
+                               "operator in %.2f s" % (M2, n, dt)}
+    return blk
 
 
 def cpu_baseline(prob, target_s):
@@ -745,6 +843,8 @@ def run_ours(a):
             "max_abs_diff_vs_c128_over_mu0": float(np.max(np.abs(mu_f.cpu().numpy() - mu_h))
                                                    / np.max(np.abs(mu_h[:, 0]))),
             "note": "dtype KPM_C128F: every real as a float pair (~48 bits), FP32 pipe; opt-in"}
+    if a.dtype == "c128" and not a.no_time:
+        line["time_evolution"] = run_time_evolution(a, op, n, L, prob, hbm_peak, world)
     clocks = clk.summary()
     if clocks is not None:
         line["clocks"] = clocks

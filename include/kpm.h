@@ -94,6 +94,10 @@ int kpm_ell_check(kpm_ell* h, void* stream);
  * thread per tile; CTAs; measured us per step. */
 int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                         float* step_us);
+/* The same for the series step (kpm_cheb_series, kpm_time_evolve, kpm_time_sigma):
+ * kind 0 = grid-stride or 2 = producer warp, timed on the operator at first use. */
+int kpm_ell_series_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
+                          float* step_us);
 /* Doubling (opt-in: KPM_FLAG_DOUBLING at creation or kpm_ell_set_doubling).
  * kpm_ell_create checks on the device whether H == H^dagger exactly (entry by
  * entry, duplicate slots summed).  For such an operator with doubling on, moment
@@ -143,6 +147,18 @@ int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r,
  */
 int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const double* v,
                     double* out, void* stream);
+
+/*
+ * Time evolution by a repeated series: out[r] = P(H)^steps v[r] with
+ * P(H) = sum_{m<M} c[m] T_m(H) (c: the time-step moments of exp(-i H dt)),
+ * steps >= 0 (0 copies v).  c: device [M] c128; v, out: device [R][n] c128; out
+ * may alias v.  The R vectors advance together, one pass over H per order.
+ * dtype KPM_C64 carries the vectors in complex64 between steps.
+ * Replaces for_time (jclsquant/cuda_cython/cuda/obv.cu:93-122), which advances
+ * U and U_c (R = 2) by len_t calls of the device rec_A each.
+ */
+int kpm_time_evolve(kpm_ell* h, int dtype, int R, int M, const double* c, int steps,
+                    const double* v, double* out, void* stream);
 
 /*
  * Commutator series out[r] = sum_m c[m] C_m with C_0 = 0, C_1 = V v,
@@ -263,15 +279,59 @@ int kpm_batch_check(kpm_batch* b, void* stream);
 int kpm_cheb_moments_noalloc(const double* data, const int32_t* indices, int len_row, int64_t n,
                              const double* v, int M, double* mu, void* stream);
 
+/* ---- operator construction on the device ---------------------------------
+ * kpm_csr_row_max: len_row = max_i (indptr[i+1] - indptr[i]) of a device CSR
+ *   (KPM_ERR_SHAPE when indptr decreases).
+ * kpm_csr_to_ell: data_indices_c (jclsquant/cython_modules/Extra_funs.pyx:81-137,
+ *   called from jclsquant/ell_matrix.py:187-200) on the GPU.  Padded row-major ELL
+ *   arrays from device CSR arrays (indptr int64 [n+1], indices int32, data c128):
+ *   row i holds its entries in stored order in slots 0..nnz_i-1; padding slots get
+ *   value 0, valid 0 and the row's last stored column (its own index for a row
+ *   without entries, where the reference reads out of bounds).  dx, dy (c128) and
+ *   conj (int32) are companions with the same sparsity, laid out alike; each output
+ *   may be NULL.  KPM_ERR_SHAPE if a row is longer than len_row.  Synchronous.
+ * kpm_honeycomb_ell: nearest-neighbour graphene on nx x ny primitive cells, the
+ *   arrays of the O(N) host builder (site 2 (iy nx + ix) + s; A bonds to B(ix, iy),
+ *   B(ix-1, iy), B(ix, iy-1), B to A(ix, iy), A(ix+1, iy), A(ix, iy+1); periodic or
+ *   open).  len_row 4: slot 0 = on-site energy onsite[i] (device [n] doubles), then
+ *   the bonds; len_row 3: bonds only (onsite unused).  disp: host [3][2], x_j - x_i
+ *   of the three A->B bonds.  Outputs (device, [n][len_row]): data c128 (t on bonds),
+ *   indices, and optional valid, dx, dy (c128), partner (int64: flat slot of the
+ *   reverse bond, -1 for on-site and padding).  Replaces the reference's setup route
+ *   lattice_hexagonal + H_graphene (jclsquant/lattice.py:6-47, jclsquant/hams.py:63-168)
+ *   for its graphene configurations.
+ * kpm_ell_gershgorin_partner: the symmetric Gershgorin bound b (host out) of such
+ *   arrays: c_j = diagonal, r_j = sum_i |H_ij| - |c_j| (column sums, each in flat slot
+ *   order through partner), b = max(|min(c - r)|, |max(c + r)|) * factor.
+ *   Bit-identical to the host builder's bound for real values.  Synchronous.
+ * kpm_ell_scale_values: data[k] *= scale (both components), modifier_bounds for
+ *   symmetric bounds (jclsquant/modifiers.py:14-36) with scale = 1 / b.
+ */
+int kpm_csr_row_max(int64_t n, const int64_t* indptr, int* len_row, void* stream);
+int kpm_csr_to_ell(int64_t n, int len_row, const int64_t* indptr, const int32_t* indices,
+                   const double* data, const double* dx, const double* dy, const int32_t* conj,
+                   double* ell_data, int32_t* ell_indices, double* ell_dx, double* ell_dy,
+                   int32_t* ell_conj, int32_t* valid, void* stream);
+int kpm_honeycomb_ell(int nx, int ny, int periodic, double t, const double* onsite, int len_row,
+                      const double* disp, double* data, int32_t* indices, int32_t* valid,
+                      double* dx, double* dy, int64_t* partner, void* stream);
+int kpm_ell_gershgorin_partner(int64_t n, int len_row, const double* data, const int32_t* indices,
+                               const int64_t* partner, double factor, double* bound, void* stream);
+int kpm_ell_scale_values(int64_t count, double scale, double* data, void* stream);
+
 /* ---- reference-compatible host-pointer entry points ---------------------
- * Same names and argument lists as jclsquant/cuda_cython/cuda/obv.h:21-23,30,
+ * Same names and argument lists as jclsquant/cuda_cython/cuda/obv.h:21-23,27,30,
  * where std::complex<double>* is passed as double* (identical layout).
  * Host buffers in and out; synchronous; the operator is uploaded per call,
  * as in the reference.  Status: kpm_last_status() (per host thread).
+ * for_time updates U and U_c in place (len_t <= 0 leaves them unchanged, as the
+ * reference's loop does).
  */
 void rec_A_tab(double* data, int* indices, int len_row, int N, double* A_vec, double* v, int M);
 void rec_A_tab_2(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l,
                  double* v_r, int M);
+void for_time(double* data, int* indices, int len_row, int N, double* moments_kernel, int len_t,
+              double* U, double* U_c, int M);
 void for_time_sigma(double* data, double* data2, double* data3, int* indices, int len_row, int N,
                     double* moments_kernel_U, double* moments_kernel_FD, int len_t,
                     double* sigma_vec, double* v, int M, int M2);

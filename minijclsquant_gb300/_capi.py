@@ -49,13 +49,17 @@ SIGNATURES = {
     "kpm_ell_check": (_I, [_P, _P]),
     "kpm_ell_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                  ctypes.POINTER(ctypes.c_float)]),
+    "kpm_ell_series_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
+                                   ctypes.POINTER(ctypes.c_float)]),
     "kpm_ell_dot": (_I, [_P, _D, _D, _D, _D, _P, _P, _I, _P]),
     "kpm_cheb_moments": (_I, [_P, _I, _I, _I, _P, _P, _P, _P, _P]),
     "kpm_cheb_series": (_I, [_P, _I, _I, _I, _P, _P, _P, _P]),
+    "kpm_time_evolve": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P]),
     "kpm_cheb_commutator_series": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _P]),
     "kpm_time_sigma": (_I, [_P, _P, _P, _I, _I, _P, _I, _P, _I, _I, _P, _P, _P]),
     "rec_A_tab": (None, [_P, _P, _I, _I, _P, _P, _I]),
     "rec_A_tab_2": (None, [_P, _P, _I, _I, _P, _P, _P, _I]),
+    "for_time": (None, [_P, _P, _I, _I, _P, _I, _P, _P, _I]),
     "for_time_sigma": (None, [_P, _P, _P, _P, _I, _I, _P, _P, _I, _P, _P, _I, _I]),
     "kpm_last_status": (_I, []),
     "kpm_ell_set_values": (_I, [_P, _P, _U, _P]),
@@ -73,6 +77,11 @@ SIGNATURES = {
     "kpm_adjoint_backward_ex": (_I, [_P, _P, _P, _I, _P]),
     "kpm_batch_props": (_I, [_P, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "kpm_batch_set_doubling": (_I, [_P, _I]),
+    "kpm_csr_row_max": (_I, [_I64, _P, ctypes.POINTER(_I), _P]),
+    "kpm_csr_to_ell": (_I, [_I64, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "kpm_honeycomb_ell": (_I, [_I, _I, _I, _D, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "kpm_ell_gershgorin_partner": (_I, [_I64, _I, _P, _P, _P, _D, ctypes.POINTER(_D), _P]),
+    "kpm_ell_scale_values": (_I, [_I64, _D, _P, _P]),
     "kpm_batch_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                    ctypes.POINTER(ctypes.c_float), _P]),
     "kpm_batch_check": (_I, [_P, _P]),

@@ -95,12 +95,12 @@ int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams&
   return f32 ? launch_step_f32(real, R, mode, epi, p, grid, s) : launch_step_f64(real, R, mode, epi, p, grid, s);
 }
 
-int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s) {
+int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s, bool series) {
   if (cfg.kind == 1)
     return f32 ? launch_staged_f32(real, R, cfg.U, p, cfg.grid, s) : launch_staged_f64(real, R, cfg.U, p, cfg.grid, s);
   if (cfg.kind == 2)
     return f32 ? launch_ws_f32(real, R, cfg.U, p, cfg.grid, s) : launch_ws_f64(real, R, cfg.U, p, cfg.grid, s);
-  return launch_step(f32, real, R, MODE_NEXT, EPI_STORE | EPI_MOM1, p, cfg.grid, s);
+  return launch_step(f32, real, R, MODE_NEXT, EPI_STORE | (series ? EPI_SERIES : EPI_MOM1), p, cfg.grid, s);
 }
 
 // Choose the MODE_NEXT kernel for (precision, R group, moment sets): the
@@ -109,6 +109,9 @@ int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepPar
 // resident CTAs.  When several fit, each is timed on the operator itself (a few
 // launches on zeroed workspace vectors) and the fastest is kept for the
 // handle's lifetime.  KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2 forces one.
+// sets: 1 one moment set, 2 two sets, 3 doubled moments, 4 a series step (no
+// moments; series += c_m T_{m+1}).  Timing clears ws.ta, ws.tb and ws.vl (and ws.vr
+// for sets 2 and 3): callers tune before they fill those.
 int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out) {
   const int key = (f32 ? 1000 : 0) + Rg * 10 + sets;
   for (auto& kv : h->tuned)
@@ -126,10 +129,11 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
     cands.push_back(c);
   }
   // the staged kernel serves one moment set; two-set calls use the grid-stride kernel;
-  // doubled moments (sets == 3) the grid-stride and the producer-warp kernels
+  // doubled moments (sets == 3) and series steps (sets == 4) the grid-stride and the
+  // producer-warp kernels
   for (int kind = 1; kind <= 2 && sets != 2; ++kind)
     for (int U = 1; U <= 2; ++U) {
-      if (sets == 3 && kind == 1) continue;
+      if ((sets == 3 || sets == 4) && kind == 1) continue;
       if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
       const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2)
                                        : staged_ctas_f64(h->is_real, Rg, U, h->L, 2))
@@ -155,29 +159,36 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
     Workspace& ws = h->ws;
     KPM_TRY(ensure(ws.ta, vb));
     KPM_TRY(ensure(ws.tb, vb));
+    const bool uses_vr = sets == 2 || sets == 3;
     KPM_TRY(ensure(ws.vl, vb));
-    if (sets >= 2) KPM_TRY(ensure(ws.vr, vb));
+    if (uses_vr) KPM_TRY(ensure(ws.vr, vb));
     KPM_TRY(ensure(ws.part, (size_t)kChunk * std::min(sets, 2) * max_grid * Rg * sizeof(double2)));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.ta.p, 0, vb, s));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.tb.p, 0, vb, s));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.vl.p, 0, vb, s));
-    if (sets >= 2) KPM_CUDA_TRY(cudaMemsetAsync(ws.vr.p, 0, vb, s));
+    if (uses_vr) KPM_CUDA_TRY(cudaMemsetAsync(ws.vr.p, 0, vb, s));
+    if (sets == 4) KPM_CUDA_TRY(cudaMemsetAsync(ws.part.p, 0, sizeof(double2), s));
     StepParams p = base_params(h, f32);
     p.tcur = ws.ta.p;
     p.tout = ws.tb.p;
-    p.vl = sets == 3 ? nullptr : ws.vl.p;
+    p.vl = (sets == 3 || sets == 4) ? nullptr : ws.vl.p;
     p.vl2 = sets == 2 ? ws.vr.p : nullptr;
     p.dbl = sets == 3;
     p.hv = sets == 3 ? ws.vr.p : nullptr;
     p.part = static_cast<double2*>(ws.part.p);
+    if (sets == 4) {  // series into ws.vl with a zero coefficient
+      p.series = ws.vl.p;
+      p.coef = static_cast<const double2*>(ws.part.p);
+      p.m = 0;
+    }
     cudaEvent_t e0, e1;
     KPM_CUDA_TRY(cudaEventCreate(&e0));
     KPM_CUDA_TRY(cudaEventCreate(&e1));
     const int reps = 3;
     for (auto& c : cands) {
-      KPM_TRY(launch_next(f32, h->is_real, Rg, c, p, s));
+      KPM_TRY(launch_next(f32, h->is_real, Rg, c, p, s, sets == 4));
       KPM_CUDA_TRY(cudaEventRecord(e0, s));
-      for (int r = 0; r < reps; ++r) KPM_TRY(launch_next(f32, h->is_real, Rg, c, p, s));
+      for (int r = 0; r < reps; ++r) KPM_TRY(launch_next(f32, h->is_real, Rg, c, p, s, sets == 4));
       KPM_CUDA_TRY(cudaEventRecord(e1, s));
       KPM_CUDA_TRY(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -564,6 +575,10 @@ int series_packed(kpm_ell_s* h, bool f32, int Rg, int M, const double2* coef, co
   const int vpt = vpt_for(f32, Rg);
   const int grid = grid_for(h, Rg, vpt);
   const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+  // tune the series step first: its timing clears ws.ta / ws.tb / ws.vl (x is never
+  // one of them; result may be ws.vl, which the first step overwrites)
+  StepConfig cfg;
+  if (M > 2) KPM_TRY(step_config(h, f32, Rg, 4, s, &cfg));
   KPM_TRY(ensure(h->ws.ta, vb));
   KPM_TRY(ensure(h->ws.tb, vb));
   KPM_CUDA_TRY(cudaMemcpyAsync(h->ws.ta.p, x, vb, cudaMemcpyDeviceToDevice, s));
@@ -576,13 +591,16 @@ int series_packed(kpm_ell_s* h, bool f32, int Rg, int M, const double2* coef, co
   KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_FIRST, EPI_STORE | EPI_SERIES, p, grid, s));
   void* tprev = h->ws.ta.p;
   void* tcur = h->ws.tb.p;
+  cudaEvent_t ev = nullptr;
+  if (M > 2) KPM_TRY(prof_begin(h, s, &ev));
   for (int m = 2; m < M; ++m) {
     p.tcur = tcur;
     p.tout = tprev;
     p.m = m;
-    KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_NEXT, EPI_STORE | EPI_SERIES, p, grid, s));
+    KPM_TRY(launch_next(f32, h->is_real, Rg, cfg, p, s, true));
     std::swap(tprev, tcur);
   }
+  if (M > 2) KPM_TRY(prof_end(h, s, ev, M - 2));
   return KPM_OK;
 }
 
@@ -838,6 +856,32 @@ int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const 
   return KPM_OK;
 }
 
+int kpm_time_evolve(kpm_ell* h, int dtype, int R, int M, const double* c, int steps, const double* v, double* out,
+                    void* stream) {
+  if (!h || !c || !v || !out || R < 1 || M < 2 || steps < 0) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  const bool f32 = dtype == KPM_C64;
+  cudaStream_t s = as_stream(stream);
+  if (f32) KPM_TRY(ensure_f32_values(h, s));
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = pow2_group(R - r0);
+    const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+    KPM_TRY(ensure(h->ws.tc, vb));
+    KPM_TRY(ensure(h->ws.acc, vb));
+    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, f32, h->ws.tc.p, s));
+    // The state ping-pongs between tc and acc: each step reads one and writes the other.
+    void* x = h->ws.tc.p;
+    void* y = h->ws.acc.p;
+    for (int j = 0; j < steps; ++j) {
+      KPM_TRY(series_packed(h, f32, Rg, M, reinterpret_cast<const double2*>(c), x, y, s));
+      std::swap(x, y);
+    }
+    KPM_TRY(unpack_vectors(x, f32, h->n, h->n_pad, R, r0, Rg, out, s));
+    r0 += Rg;
+  }
+  return KPM_OK;
+}
+
 int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M, const double* c, const double* v,
                                double* out, void* stream) {
   if (!h || !v_op || !c || !v || !out || R < 1 || M < 2) return KPM_ERR_INVALID_ARG;
@@ -931,6 +975,19 @@ int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_t
   return KPM_OK;
 }
 
+int kpm_ell_series_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid, float* step_us) {
+  if (!h || R < 1) return KPM_ERR_INVALID_ARG;
+  KPM_TRY(check_dtype(dtype));
+  if (dtype == KPM_C64) KPM_TRY(ensure_f32_values(h, nullptr));
+  StepConfig cfg;
+  KPM_TRY(step_config(h, dtype == KPM_C64, pow2_group(R), 4, nullptr, &cfg));
+  if (kind) *kind = cfg.kind;
+  if (rows_per_thread) *rows_per_thread = cfg.U;
+  if (grid) *grid = cfg.grid;
+  if (step_us) *step_us = cfg.us;
+  return KPM_OK;
+}
+
 int kpm_ell_props(const kpm_ell* h, int* hermitian, int* doubling) {
   if (!h) return KPM_ERR_INVALID_ARG;
   if (hermitian) *hermitian = h->hermitian;
@@ -979,6 +1036,43 @@ void rec_A_tab(double* data, int* indices, int len_row, int N, double* A_vec, do
 
 void rec_A_tab_2(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l, double* v_r, int M) {
   g_last_status = host_rec(data, indices, len_row, N, A_vec, v_l, v_r, M);
+}
+
+void for_time(double* data, int* indices, int len_row, int N, double* moments_kernel, int len_t, double* U,
+              double* U_c, int M) {
+  if (!data || !indices || !moments_kernel || !U || !U_c || N < 1 || len_row < 1 || M < 2) {
+    g_last_status = KPM_ERR_INVALID_ARG;
+    return;
+  }
+  if (len_t <= 0) {  // the reference's loop runs no step and copies U, U_c back unchanged
+    g_last_status = KPM_OK;
+    return;
+  }
+  kpm_ell* h = nullptr;
+  int st = kpm_ell_create(&h, N, len_row, data, indices, 0u, nullptr);
+  DevBuf dc, dv;
+  const size_t nb = (size_t)N * sizeof(double2);
+  if (st == KPM_OK) st = ensure(dc, (size_t)M * sizeof(double2));
+  if (st == KPM_OK) st = ensure(dv, 2 * nb);
+  cudaError_t e = cudaSuccess;
+  char* dvp = static_cast<char*>(dv.p);
+  if (st == KPM_OK) e = cudaMemcpy(dc.p, moments_kernel, (size_t)M * sizeof(double2), cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(dvp, U, nb, cudaMemcpyHostToDevice);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(dvp + nb, U_c, nb, cudaMemcpyHostToDevice);
+  // U and U_c advance as one group of two vectors: one pass over H per order for both.
+  if (st == KPM_OK && e == cudaSuccess)
+    st = kpm_time_evolve(h, KPM_C128, 2, M, static_cast<double*>(dc.p), len_t, static_cast<double*>(dv.p),
+                         static_cast<double*>(dv.p), nullptr);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(U, dvp, nb, cudaMemcpyDeviceToHost);
+  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(U_c, dvp + nb, nb, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    st = KPM_ERR_CUDA;
+  }
+  release(dc);
+  release(dv);
+  if (h) kpm_ell_destroy(h);
+  g_last_status = st;
 }
 
 void for_time_sigma(double* data, double* data2, double* data3, int* indices, int len_row, int N,

@@ -167,7 +167,8 @@ int pow2_group(int remaining);
 int vpt_for(bool f32, int Rg);
 StepParams base_params(kpm_ell_s* h, bool f32);
 int launch_step(bool f32, bool real, int R, int mode, int epi, const StepParams& p, int grid, cudaStream_t s);
-int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s);
+int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepParams& p, cudaStream_t s,
+                bool series = false);
 int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out);
 // Doubling: whether a DOS moment call on h uses it; |v|^2 / 2 of a packed set; the
 // Hermitian check run at creation; the assembly of mu from the reduced sets.

@@ -11,6 +11,10 @@
 // neighbour gathers T_m[col] the others compute, and the producer refills a
 // stage as soon as the last warp has left it.
 //
+// The SER instantiation is a series step of rec_A_vec (p.series set, p.vl null, no
+// doubling): the producer stages the series accumulator tile in the left-vector
+// slot and the compute warps write back series + c_m T_{m+1}; no moments are formed.
+//
 // Moment partials follow the staged kernel: per CTA (strided tiles) or, for
 // batched operators (per_tile), flushed per (CTA, instance) run with a block
 // reduction over the compute warps alone (named barrier 1).  With p.vl null the
@@ -33,7 +37,7 @@ namespace kpm {
 constexpr int kWsStages = 4;
 constexpr int kWsThreads = kBlock + 32;  // compute warps + one producer warp
 
-template <typename T, bool REAL, int TPR, int VPT, int U>
+template <typename T, bool REAL, int TPR, int VPT, int U, bool SER>
 __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;
@@ -82,7 +86,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
       tc.col = p.col;
       tc.val = static_cast<const unsigned char*>(p.val);
       tc.old = static_cast<const unsigned char*>(p.tprev ? p.tprev : p.tout);
-      tc.vl = static_cast<const unsigned char*>(p.vl);
+      // a series step (no moments) stages the series accumulator in the left-vector slot
+      tc.vl = static_cast<const unsigned char*>(SER ? p.series : p.vl);
       tc.vl2 = nullptr;
       tc.ld = p.ld;
       tc.L = L;
@@ -116,6 +121,10 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
   int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
   const bool dbl = p.dbl != 0;
   const bool mom = p.vl != nullptr || dbl;
+  // series step: series += c_m T_{m+1} (rec_A_vec), the accumulator tile staged like v_l
+  constexpr bool ser = SER;
+  Raw* series = static_cast<Raw*>(p.series);
+  const double2 cm = ser ? p.coef[p.m] : make_double2(0.0, 0.0);
   const int64_t set_stride = p.per_tile ? p.part_set_stride : (int64_t)gridDim.x * R;
 
   const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
@@ -203,7 +212,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
           const T* shv = reinterpret_cast<const T*>(svl) + ((u * RPB + rl) * TPR + sub) * VPT;
 #pragma unroll
           for (int q = 0; q < VPT; ++q) hvs[u][q] = shv[q];
-        } else if (mom) {
+        } else if (mom || ser) {
           unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
         }
       }
@@ -214,6 +223,17 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
       for (int u = 0; u < U; ++u) {
         const int64_t vi = (row0 + u * RPB + rl) * TPR + sub;
         tout[vi] = pack(acc[u]);
+        if (ser) {
+          Cx<T, VPT> o;
+#pragma unroll
+          for (int q = 0; q < VPT; ++q) {
+            // y = c_m*x + 1*y, the expression of the grid-stride kernel
+            o.re[q] = ((T)cm.x * acc[u].re[q] - (T)cm.y * acc[u].im[q]) + l[u].re[q];
+            o.im[q] = ((T)cm.x * acc[u].im[q] + (T)cm.y * acc[u].re[q]) + l[u].im[q];
+          }
+          series[vi] = pack(o);
+          continue;
+        }
         if (!mom) continue;
         if (dbl) {
           Cx<T, VPT> own;  // T_m at this row
@@ -263,11 +283,11 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
   }
 }
 
-template <typename T, bool REAL, int TPR, int VPT, int U>
+template <typename T, bool REAL, int TPR, int VPT, int U, bool SER>
 bool ws_smem_attr(size_t smem) {
   static size_t configured = 0;
   if (smem <= configured) return true;
-  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U>,
+  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, SER>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -281,8 +301,13 @@ bool ws_smem_attr(size_t smem) {
 template <typename T, bool REAL, int TPR, int VPT, int U>
 int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
-  if (!ws_smem_attr<T, REAL, TPR, VPT, U>(smem)) return KPM_ERR_UNSUPPORTED;
-  cheb_next_ws_kernel<T, REAL, TPR, VPT, U><<<grid, kWsThreads, smem, s>>>(p);
+  if (p.series && !p.vl && !p.dbl) {
+    if (!ws_smem_attr<T, REAL, TPR, VPT, U, true>(smem)) return KPM_ERR_UNSUPPORTED;
+    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, true><<<grid, kWsThreads, smem, s>>>(p);
+  } else {
+    if (!ws_smem_attr<T, REAL, TPR, VPT, U, false>(smem)) return KPM_ERR_UNSUPPORTED;
+    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, false><<<grid, kWsThreads, smem, s>>>(p);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -295,9 +320,9 @@ template <typename T, bool REAL, int TPR, int VPT, int U>
 int ws_ctas_per_sm(int L, int nvec) {
   const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
   if (smem > 200 * 1024) return 0;
-  if (!ws_smem_attr<T, REAL, TPR, VPT, U>(smem)) return 0;
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U, false>(smem)) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U>, kWsThreads,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, false>, kWsThreads,
                                                     smem) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;

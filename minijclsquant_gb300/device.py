@@ -189,6 +189,23 @@ def cheb_series(op: DeviceELL, M: int, c, v, dtype="c128", stream=None):
     return _finish(out, squeeze, was_np)
 
 
+def time_evolve(op: DeviceELL, M: int, c, steps: int, v, dtype="c128", stream=None):
+    """P(H)^steps v with P(H) = sum_{m<M} c[m] T_m(H) (for_time, obv.cu:93-122); all
+    vectors of v advance together."""
+    M, steps = int(M), int(steps)
+    if M < 2:
+        raise ValueError("M must be >= 2")
+    if steps < 0:
+        raise ValueError("steps must be >= 0")
+    tv, R, squeeze, was_np = _vectors(v, op.n)
+    tc = _coef(c, M, tv.device)
+    out = torch.empty_like(tv)
+    st = _capi.lib().kpm_time_evolve(op.handle, _capi.dtype_code(dtype), R, M, tc.data_ptr(), steps, tv.data_ptr(),
+                                     out.data_ptr(), _stream_ptr(stream))
+    _capi.check(st, "kpm_time_evolve")
+    return _finish(out, squeeze, was_np)
+
+
 def cheb_commutator_series(op: DeviceELL, vop: DeviceELL, M: int, c, v, stream=None):
     """out = sum_m c[m] C_m with the commutator recursion (rec_com_A_vec)."""
     M = int(M)

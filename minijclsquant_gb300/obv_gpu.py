@@ -48,6 +48,19 @@ def rec_A_tab_2_gpu(data, indices, len_row, v_l, v_r, A_vec, M):
     _status("rec_A_tab_2")
 
 
+def for_time_gpu(data, indices, len_row, moments_kernel, len_t, U, U_c, M):
+    """U, U_c <- (sum_m c_m T_m)^len_t applied to each, in place (obv.pyx:52-62 -> obv.cu:93-122)."""
+    _c128(data, "data"), _i32(indices, "indices"), _c128(moments_kernel, "moments_kernel")
+    _c128(U, "U"), _c128(U_c, "U_c")
+    if U_c.shape[0] != U.shape[0]:
+        raise ValueError("U and U_c differ in length")
+    if moments_kernel.size < M:
+        raise ValueError("moments_kernel is shorter than M")
+    _capi.lib().for_time(data.ctypes.data, indices.ctypes.data, int(len_row), int(U.shape[0]),
+                         moments_kernel.ctypes.data, int(len_t), U.ctypes.data, U_c.ctypes.data, int(M))
+    _status("for_time")
+
+
 def for_time_sigma_gpu(data, data2, data3, indices, len_row, moments_kernel_U, moments_kernel_FD, len_t, sigma_vec,
                        v, M, M2):
     """sigma_vec[j] = <U_c(t_j)|V1 U(t_j)> (obv.pyx:66-75 -> obv.cu:124-176)."""

@@ -116,6 +116,16 @@ def rec_A_vec(M, data, indices, len_row, c, v, threads=None):
     return out
 
 
+def for_time(data, indices, len_row, c, len_t, U, U_c, M, threads=None):
+    """(U, U_c) after len_t applications of sum_m c_m T_m to each (obv.cu:93-122: the
+    loop over len_t calling the device rec_A, recursions.cu:267-317, on U and on U_c)."""
+    U, U_c = _c(U, np.complex128).copy(), _c(U_c, np.complex128).copy()
+    for _ in range(int(len_t)):
+        U = rec_A_vec(M, data, indices, len_row, c, U, threads)
+        U_c = rec_A_vec(M, data, indices, len_row, c, U_c, threads)
+    return U, U_c
+
+
 def rec_com_A_vec(M, data_a, data_v, indices, len_row, c, v, threads=None):
     """Commutator series (recurrence_functions.py:146-196); A and V share `indices`."""
     data_a, data_v = _c(data_a, np.complex128), _c(data_v, np.complex128)

@@ -172,6 +172,42 @@ def main():
          delta=np.stack([km.moments_delta(e, 32) for e in E]), fd_t0=np.stack([km.moments_FD_T0(e, 32) for e in E]),
          mu_U=km.moments_U(1.3, 40), gmas=np.stack([km.moments_Gmas(e, 16) for e in E]))
 
+    time_evolution_case(ref)
+
+
+def time_evolution_case(ref):
+    """8. time evolution (for_time, jclsquant/cuda_cython/cuda/obv.cu:93-122): len_t times
+    U <- sum_m c_m T_m U and U_c <- sum_m c_m T_m U_c with the time-step moments of
+    exp(-i H dt).  The device rec_A it calls (recursions.cu:267-317) is the recursion of
+    the reference's CPU rec_A_vec (recurrence_functions.py:114-143), which runs here.
+    The operator has complex (Peierls-like) hoppings and open boundaries."""
+    rf = ref.recurrence_functions
+    km = ref.kernel_and_moments
+    arr = lattice.honeycomb_arrays(6, 5, t=-2.7, W=0.4, seed=31, periodic=False)
+    phase = np.exp(1j * 0.5 * np.real(arr["dx"]) / 0.142)
+    arr_c = dict(arr, data=np.where(np.real(arr["dx"]) != 0, arr["data"] * phase, arr["data"]))
+    H = ref.ell_matrix.ell_matrix(lattice.to_csr(arr_c))
+    H_kpm = H.modifier(ref.modifiers.modifier_bounds)
+    n = int(H.shape[0])
+    M, len_t, dt = 24, 5, 0.9
+    c = km.moments_U(dt, M).astype(np.complex128)
+    U0 = ref.observables.random_vector_generator(n, 501)
+    Uc0 = ref.observables.random_vector_generator(n, 502)
+    U, Uc = U0.copy(), Uc0.copy()
+    for _ in range(len_t):
+        U = rf.rec_A_vec(M, H_kpm, c, U)
+        Uc = rf.rec_A_vec(M, H_kpm, c, Uc)
+    save("time_evolution_6x5", data_kpm=H_kpm.data, indices=H.indices, len_row=np.int64(H.len_row),
+         n=np.int64(n), c=c, M=np.int64(M), len_t=np.int64(len_t), U0=U0, Uc0=Uc0, U=U, Uc=Uc)
+
+
+CASES = {"time_evolution_6x5": time_evolution_case}
+
 
 if __name__ == "__main__":
-    main()
+    # With case names as arguments only those cases are rewritten; with none, all of them.
+    if len(sys.argv) > 1:
+        for name in sys.argv[1:]:
+            CASES[name](reference_import.load())
+    else:
+        main()

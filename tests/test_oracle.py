@@ -50,6 +50,16 @@ def test_oracle_other_recursions_match_reference():
     assert np.max(np.abs(sig - x["sigma"])) <= 1e-11 * np.max(np.abs(x["sigma"]))
 
 
+def test_oracle_time_evolution_matches_reference():
+    z = golden("time_evolution_6x5")
+    U, Uc = oracle.for_time(z["data_kpm"], z["indices"], int(z["len_row"]), z["c"], int(z["len_t"]), z["U0"],
+                            z["Uc0"], int(z["M"]))
+    assert np.max(np.abs(U - z["U"])) <= 1e-13 * np.max(np.abs(z["U"]))
+    assert np.max(np.abs(Uc - z["Uc"])) <= 1e-13 * np.max(np.abs(z["Uc"]))
+    # exp(-i H dt) is unitary and the moments are converged: norms are kept
+    assert abs(np.linalg.norm(z["U"]) - np.linalg.norm(z["U0"])) <= 1e-10 * np.linalg.norm(z["U0"])
+
+
 def test_oracle_tiny_and_short_recursions():
     z = golden("tiny_2x2")
     L = int(z["len_row"])

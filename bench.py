@@ -64,6 +64,11 @@ def parse():
     ap.add_argument("--adj-cells", type=int, default=512)
     ap.add_argument("--adj-M", type=int, default=1024)
     ap.add_argument("--adj-fd", type=int, default=64, help="parameters checked by central differences")
+    ap.add_argument("--no-setup", action="store_true", help="skip the operator-construction measurement")
+    ap.add_argument("--no-sigma", action="store_true", help="skip the time-domain Kubo (for_time_sigma) measurement")
+    ap.add_argument("--sigma-cells", type=int, default=1024)
+    ap.add_argument("--sigma-M", type=int, default=512, help="Fermi-Dirac (commutator series) terms")
+    ap.add_argument("--sigma-len-t", type=int, default=32)
     ap.add_argument("--no-time", action="store_true", help="skip the time-evolution (for_time) measurement")
     ap.add_argument("--time-M", type=int, default=64, help="series terms per time step")
     ap.add_argument("--time-len", type=int, default=8, help="time steps per timed step")
@@ -296,6 +301,131 @@ def run_time_evolution(a, op, n, L, prob, hbm_peak, world):
                                "kind": kind_s, "sample": "one time step of U and U_c (M2=%d) on the full %d-site "
                                "operator in %.2f s" % (M2, n, dt)}
     return blk
+
+
+def run_setup(a, prob, host_s, hbm_peak):
+    """Operator construction for the DOS lattice: the host route (numpy builder, Gershgorin
+    bound, modifier_bounds, upload and kpm_ell_create; host_s) against the device builder
+    (on-site energies on the host, then kpm_honeycomb_ell, kpm_ell_gershgorin_partner,
+    kpm_ell_scale_values and kpm_ell_create from device arrays), both to a ready handle.
+    The generator kernel is timed alone with CUDA events: it writes data (16 B), column
+    (4 B), valid (4 B) and partner (8 B) per slot and reads one on-site energy per site."""
+    import torch
+
+    from minijclsquant_gb300 import _capi, lattice
+
+    kw = dict(t=-2.7, W=a.W, seed=1234, bounds_factor=1.01)
+    lattice.honeycomb_device(64, 64, **kw)  # first launches, allocator warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    g = lattice.honeycomb_device(a.cells, a.cells, **kw)
+    torch.cuda.synchronize()
+    dev_s = time.perf_counter() - t0
+    same = bool(np.array_equal(g.bounds, prob["bounds"])) and bool(
+        torch.equal(g.data_kpm, torch.from_numpy(prob["data_kpm"]).cuda())) and bool(
+        torch.equal(g.indices, torch.from_numpy(prob["indices"]).cuda()))
+    n, L = g.n, g.len_row
+    eps = torch.from_numpy(lattice._onsite_energies(n, a.W, 1234, 0.0, None)[0]).cuda()
+    disp = np.ascontiguousarray(lattice._bond_displacements(lattice.A_CC).reshape(-1))
+    lib = _capi.lib()
+    stream = torch.cuda.current_stream()
+    sp = ctypes_stream(stream)
+    reps = 5
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        _capi.check(lib.kpm_honeycomb_ell(a.cells, a.cells, 1, -2.7, eps.data_ptr(), L, disp.ctypes.data,
+                                          g.data.data_ptr(), g.indices.data_ptr(), g.valid.data_ptr(), None, None,
+                                          g.partner.data_ptr(), sp), "kpm_honeycomb_ell")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    k_s = e0.elapsed_time(e1) * 1e-3 / reps
+    bytes_k = float(n) * (L * (16 + 4 + 4 + 8) + 8)
+    gbs = bytes_k / k_s / 1e9
+    del g
+    torch.cuda.empty_cache()
+    return {"sites": n, "host_route_s": host_s, "device_route_s": dev_s, "speedup": host_s / dev_s,
+            "bit_identical": same,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                         "kernel": "honeycomb_kernel", "algorithmic_bytes_per_launch": bytes_k,
+                         "avg_launch_ms": k_s * 1e3},
+            "note": "host route: honeycomb_arrays + gershgorin_bounds_ell + modifier_bounds + DeviceELL upload; "
+                    "device route: lattice.honeycomb_device (both end at a ready operator handle)"}
+
+
+def run_time_sigma(a, hbm_peak, world):
+    """Time-domain Kubo correlator sigma(t_j) = <U_c(t_j)|V1 U(t_j)> (for_time_sigma,
+    obv.cu:124-176; the historical kpm_sigma_time_gpu): U_c(0) = the commutator series of
+    the Fermi-Dirac moments (M terms, V2 = H o dx / a), then U and U_c advanced len_t - 1
+    times by the exp(-i H dt) series (M2 terms, truncated where |c_m| <= 1e-15) and
+    correlated with V1 = -i H o dy.  One random-phase vector, as the reference calls it.
+    Value: site-steps/s counting N per commutator order and N per series order of each of
+    U and U_c: N ((M - 1) + 2 (M2 - 1)(len_t - 1))."""
+    import torch
+
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.constants import hbar_fs
+    from minijclsquant_gb300.kernel_and_moments import JacksonKernel, moments_FD_T0, moments_U
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity, modifier_velocity_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    H = lattice.honeycomb(a.sigma_cells, a.sigma_cells, t=-2.7, W=a.W, seed=1234)
+    n, L = H.shape[0], H.len_row
+    M, len_t = a.sigma_M, a.sigma_len_t
+    t_vec = np.linspace(0, 5 * hbar_fs * M / (np.pi * H.bounds[1]), 500)
+    dt_kpm = t_vec[1] * H.bounds[1] / hbar_fs
+    cu = moments_U(dt_kpm, M)
+    M2 = 0
+    while np.abs(cu[M2]) > 1e-15 and M2 < M - 1:
+        M2 += 1
+    cu = moments_U(dt_kpm, M2).astype(np.complex128)
+    cfd = (moments_FD_T0(0.0, M) * JacksonKernel(M)).astype(np.complex128)
+    Hk = device.DeviceELL(modifier_bounds(H), H.indices, L)
+    V1 = device.DeviceELL(modifier_velocity(H, "y"), H.indices, L)
+    V2 = device.DeviceELL(modifier_velocity_bounds(H, "x"), H.indices, L)
+    v = torch.from_numpy(random_vector_generator(n, 77)).cuda()
+    for _ in range(max(1, a.warmup)):
+        sig = device.time_sigma(Hk, V1, V2, cu, M2, cfd, M, 2, v)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        sig = device.time_sigma(Hk, V1, V2, cu, M2, cfd, M, len_t, v)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world) / a.steps
+    site_steps = float(n) * ((M - 1) + 2 * (M2 - 1) * (len_t - 1))
+    blk = {"value": site_steps * world / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+           "config": {"lattice": "honeycomb %dx%d cells (%d sites), W=%g" % (a.sigma_cells, a.sigma_cells, n, a.W),
+                      "M": M, "M2": M2, "len_t": len_t, "dt_kpm": dt_kpm, "vectors": 1},
+           "gpu_launches": (M + 1) + (len_t - 1) * (M2 + 2) + 2 * len_t,
+           "sigma_0": [float(np.real(sig.cpu().numpy()[0])), float(np.imag(sig.cpu().numpy()[0]))],
+           "note": "U and U_c advance as one set of two vectors through the autotuned series step"}
+    if not a.no_cpu and world == 1:
+        from oracle import oracle
+
+        threads = os.cpu_count() or 1
+        lt = 2
+        t0 = time.perf_counter()
+        oracle.for_time_sigma(modifier_bounds(H), modifier_velocity(H, "y"), modifier_velocity_bounds(H, "x"),
+                              H.indices, L, cu, cfd, lt, v.cpu().numpy(), M, M2, threads=threads)
+        dt = time.perf_counter() - t0
+        blk["cpu_baseline"] = {"value": float(n) * ((M - 1) + 2 * (M2 - 1) * (lt - 1)) / dt, "unit": UNIT,
+                               "cores": threads, "kind": "port",
+                               "sample": "for_time_sigma restated in C (oracle), len_t=%d, same lattice and M, M2 "
+                                         "(%.2f s)" % (lt, dt)}
+    del Hk, V1, V2
+    torch.cuda.empty_cache()
+    return blk
+
+
+def ctypes_stream(stream):
+    import ctypes
+
+    return ctypes.c_void_p(int(stream.cuda_stream))
 
 
 def cpu_baseline(prob, target_s):
@@ -702,9 +832,12 @@ def run_ours(a):
 
     world, rank, local = dist_init()
     _capi.load(build_if_missing=False)
+    t_build = time.perf_counter()
     prob = build_problem(a.cells, a.W)
     n, L, M, R = prob["n"], prob["L"], a.M, a.R
     op = device.DeviceELL(prob["data_kpm"], prob["indices"], L)
+    torch.cuda.synchronize()
+    host_build_s = time.perf_counter() - t_build
     vs_host = random_vectors(n, R, 1000 + rank * R)
     v = torch.from_numpy(vs_host).cuda()
     op.reserve(a.dtype, R, M)
@@ -845,6 +978,10 @@ def run_ours(a):
             "note": "dtype KPM_C128F: every real as a float pair (~48 bits), FP32 pipe; opt-in"}
     if a.dtype == "c128" and not a.no_time:
         line["time_evolution"] = run_time_evolution(a, op, n, L, prob, hbm_peak, world)
+    if not a.no_setup:
+        line["setup"] = run_setup(a, prob, host_build_s, hbm_peak)
+    if not a.no_sigma:
+        line["time_sigma"] = run_time_sigma(a, hbm_peak, world)
     clocks = clk.summary()
     if clocks is not None:
         line["clocks"] = clocks

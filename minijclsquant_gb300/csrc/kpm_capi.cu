@@ -903,6 +903,28 @@ int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int 
   return KPM_OK;
 }
 
+// U (slots 0..Rg-1) and U_c (slots Rg..2Rg-1) of one packed set [n_pad][2 Rg], joined from
+// or split into two sets [n_pad][Rg].
+__global__ void join_split_kernel(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, int join) {
+  const int64_t total = n_pad * 2 * Rg;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / (2 * Rg);
+    const int r = (int)(t - i * 2 * Rg);
+    double2* half = r < Rg ? a : b;
+    const int64_t k = i * Rg + (r < Rg ? r : r - Rg);
+    if (join) both[t] = half[k];
+    else half[k] = both[t];
+  }
+}
+
+int join_split(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, bool join, cudaStream_t s) {
+  const int64_t total = n_pad * 2 * Rg;
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+  join_split_kernel<<<grid, 256, 0, s>>>(a, b, both, n_pad, Rg, join ? 1 : 0);
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
 int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u, int M2,
                    const double* c_fd, int M, int len_t, const double* v, double* sigma, void* stream) {
   if (!h || !v1 || !v2 || !c_u || !c_fd || !v || !sigma || R < 1 || M < 2 || M2 < 2 || len_t < 1)
@@ -912,12 +934,15 @@ int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const
   if (v1->n != h->n || v2->n != h->n) return KPM_ERR_SHAPE;
   cudaStream_t s = as_stream(stream);
   for (int r0 = 0; r0 < R;) {
-    const int Rg = pow2_group(R - r0);
+    // U and U_c advance together as one set of 2 Rg vectors: one pass over H per order
+    const int Rg = std::min(pow2_group(R - r0), kMaxGroupR / 2);
     const size_t vb = (size_t)h->n_pad * Rg * sizeof(double2);
     Workspace& ws = h->ws;
-    KPM_TRY(ensure(ws.vl, vb));   // v (input of the commutator series)
-    KPM_TRY(ensure(ws.vr, vb));   // U
-    KPM_TRY(ensure(ws.acc, vb));  // U_c
+    KPM_TRY(ensure(ws.vl, vb));       // v (input of the commutator series)
+    KPM_TRY(ensure(ws.vr, vb));       // U
+    KPM_TRY(ensure(ws.acc, vb));      // U_c
+    KPM_TRY(ensure(ws.td, 2 * vb));   // U | U_c joined (also scratch of the commutator series)
+    KPM_TRY(ensure(ws.acc2, 2 * vb)); // the next joined state (likewise)
     const int grid = grid_for(v1, Rg, 1);
     KPM_TRY(ensure(ws.part, (size_t)grid * Rg * sizeof(double2)));
     KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, false, ws.vr.p, s));
@@ -925,12 +950,16 @@ int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const
     KPM_TRY(comm_series_packed(h, v2, Rg, M, reinterpret_cast<const double2*>(c_fd),
                                static_cast<const double2*>(ws.vl.p), static_cast<double2*>(ws.acc.p), s));
     double* outs[2] = {sigma, sigma};
+    double2* cur = static_cast<double2*>(ws.td.p);
+    double2* nxt = static_cast<double2*>(ws.acc2.p);
+    double2* U = static_cast<double2*>(ws.vr.p);
+    double2* Uc = static_cast<double2*>(ws.acc.p);
     for (int j = 0; j < len_t; ++j) {
       if (j > 0) {
-        KPM_TRY(series_packed(h, false, Rg, M2, reinterpret_cast<const double2*>(c_u), ws.vr.p, ws.vl.p, s));
-        KPM_CUDA_TRY(cudaMemcpyAsync(ws.vr.p, ws.vl.p, vb, cudaMemcpyDeviceToDevice, s));
-        KPM_TRY(series_packed(h, false, Rg, M2, reinterpret_cast<const double2*>(c_u), ws.acc.p, ws.vl.p, s));
-        KPM_CUDA_TRY(cudaMemcpyAsync(ws.acc.p, ws.vl.p, vb, cudaMemcpyDeviceToDevice, s));
+        if (j == 1) KPM_TRY(join_split(U, Uc, cur, h->n_pad, Rg, true, s));
+        KPM_TRY(series_packed(h, false, 2 * Rg, M2, reinterpret_cast<const double2*>(c_u), cur, nxt, s));
+        std::swap(cur, nxt);
+        KPM_TRY(join_split(U, Uc, cur, h->n_pad, Rg, false, s));
       }
       // sigma_j = <U_c | V1 U>
       StepParams p = base_params(v1, false);

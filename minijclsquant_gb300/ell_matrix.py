@@ -57,6 +57,66 @@ def csr_to_ell_arrays(A, extra=()):
     return L, data, indices, valid, outs
 
 
+def csr_to_ell_device(A, extra=(), conjugates=None, stream=None):
+    """csr_to_ell_arrays on the GPU (kpm_csr_row_max + kpm_csr_to_ell): the same
+    padded row-major arrays, bit for bit, as CUDA tensors.  ``A`` is a scipy CSR
+    matrix (uploaded) or a tuple (indptr, indices, data) of CUDA tensors.  ``extra``
+    holds companion matrices with A's sparsity (DX, DY); ``conjugates`` an int32
+    array of the entries' conjugate slots (the reference's CJ data).  Returns
+    (len_row, data, indices, valid, [extras], conj or None)."""
+    import ctypes
+
+    import torch
+
+    from . import _capi, device
+
+    dev = torch.device("cuda")
+    if isinstance(A, tuple):
+        indptr, cols, vals = A
+        indptr = indptr.to(device=dev, dtype=torch.int64).contiguous()
+        cols = cols.to(device=dev, dtype=torch.int32).contiguous()
+        vals = vals.to(device=dev, dtype=torch.complex128).contiguous()
+        extras = [e.to(device=dev, dtype=torch.complex128).contiguous() for e in extra]
+    else:
+        A = A.tocsr()
+        indptr = torch.from_numpy(np.asarray(A.indptr, dtype=np.int64)).to(dev)
+        cols = torch.from_numpy(np.asarray(A.indices, dtype=np.int32)).to(dev)
+        vals = torch.from_numpy(np.asarray(A.data, dtype=np.complex128)).to(dev)
+        extras = []
+        for E in extra:
+            E = E.tocsr()
+            if E.nnz != A.nnz:
+                raise ValueError("companion matrix has %d entries, operator has %d" % (E.nnz, A.nnz))
+            extras.append(torch.from_numpy(np.asarray(E.data, dtype=np.complex128)).to(dev))
+    if len(extras) > 2:
+        raise ValueError("at most two companion matrices (DX, DY)")
+    cj = None
+    if conjugates is not None:
+        cj = torch.as_tensor(np.asarray(conjugates, dtype=np.int32) if not isinstance(conjugates, torch.Tensor)
+                             else conjugates).to(device=dev, dtype=torch.int32).contiguous()
+    n = int(indptr.numel() - 1)
+    lib = _capi.lib()
+    sp = device._stream_ptr(stream)
+    L = ctypes.c_int()
+    _capi.check(lib.kpm_csr_row_max(n, indptr.data_ptr(), ctypes.byref(L), sp), "kpm_csr_row_max")
+    L = int(L.value)
+    if L < 1:
+        raise ValueError("matrix without entries")
+    data = torch.empty(n * L, dtype=torch.complex128, device=dev)
+    idx = torch.empty(n * L, dtype=torch.int32, device=dev)
+    valid = torch.empty(n * L, dtype=torch.int32, device=dev)
+    outs = [torch.empty(n * L, dtype=torch.complex128, device=dev) for _ in extras]
+    cj_out = torch.empty(n * L, dtype=torch.int32, device=dev) if cj is not None else None
+    ptr = lambda t: t.data_ptr() if t is not None else None  # noqa: E731
+    src = extras + [None] * (2 - len(extras))
+    dst = outs + [None] * (2 - len(outs))
+    st = lib.kpm_csr_to_ell(n, L, indptr.data_ptr(), cols.data_ptr(), vals.data_ptr(), ptr(src[0]), ptr(src[1]),
+                            ptr(cj), data.data_ptr(), idx.data_ptr(), ptr(dst[0]), ptr(dst[1]), ptr(cj_out),
+                            valid.data_ptr(), sp)
+    _capi.check(st, "kpm_csr_to_ell")
+    return L, data, idx, valid, outs, cj_out
+
+
 def ell_to_csr(A):
     """ELL object -> scipy CSR (jclsquant/ell_matrix.py:15-31), vectorised."""
     n = int(A.shape[0])

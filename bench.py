@@ -293,6 +293,29 @@ def run_time_evolution(a, op, n, L, prob, hbm_peak, world):
            "norm_drift": drift,
            "gpu_launches": len_t * (M2 + 1) * a.steps,
            "note": "exp(-i H dt) by its Chebyshev series (moments_U); norm_drift = max |(|U(t)| - |U(0)|)| / |U(0)|"}
+    # the same workload in float-float complex128 (KPM_C128F, FP32 pipe), same memory streams
+    out_f = device.time_evolve(op, M2, c, 1, uv, dtype="c128f")  # tunes the float-float series step
+    torch.cuda.synchronize()
+    lib.kpm_ell_profile(op.handle, 1)
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(a.steps):
+        out_f = device.time_evolve(op, M2, c, len_t, uv, dtype="c128f")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    _capi.check(lib.kpm_ell_profile_read(op.handle, ctypes.byref(loop_ms), ctypes.byref(launches),
+                                         ctypes.byref(rows)))
+    lib.kpm_ell_profile(op.handle, 0)
+    ms_f = max_over_ranks(f0.elapsed_time(f1), world) / a.steps
+    step_f = loop_ms.value * 1e-3 / max(1, launches.value)
+    gbs_f = float(n) * bytes_per_row / step_f / 1e9
+    blk["c128f"] = {"value": float(n) * R2 * (M2 - 1) * len_t * world / (ms_f * 1e-3), "ms_per_step": ms_f,
+                    "roofline": {"bound": "hbm", "achieved": gbs_f, "peak": hbm_peak, "unit": "GB/s",
+                                 "frac": gbs_f / hbm_peak, "kernel": "ff_next_kernel<SER> (float-float series step)",
+                                 "avg_launch_ms": step_f * 1e3},
+                    "max_abs_diff_vs_c128_over_max": float(torch.max(torch.abs(out_f - out)) / torch.max(torch.abs(out))),
+                    "note": "dtype KPM_C128F: every real as a float pair (~48 bits), FP32 pipe; opt-in"}
     if not a.no_cpu and world == 1:
         threads = os.cpu_count() or 1
         vs = random_vectors(n, R2, 4242)

@@ -50,7 +50,8 @@ extern "C" {
 #define KPM_C128 0   /* complex128 recursion, FP64 moments (the drop-in form)   */
 #define KPM_C64 1    /* complex64 recursion and values, FP64 moment accumulation */
 #define KPM_C128F 2  /* complex128 accuracy in float-float arithmetic on the FP32 pipe
-                        (kpm_cheb_moments without mu_rr only; see there)           */
+                        (kpm_cheb_moments without mu_rr, kpm_cheb_series,
+                        kpm_time_evolve; see kpm_cheb_moments)                     */
 
 /* ---- operator creation flags ------------------------------------------- */
 #define KPM_FLAG_DEVICE_PTRS 1u   /* data/indices are device pointers        */
@@ -142,7 +143,8 @@ int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r,
 
 /*
  * out[r] = sum_{m<M} c[m] T_m(H) v[r]   (c: device [M] c128; v, out: device [R][n] c128;
- * out may alias v).  Replaces rec_A_vec (jclsquant/recurrence_functions.py:114-143)
+ * out may alias v).  dtype KPM_C128, KPM_C64 or KPM_C128F (float-float arithmetic,
+ * within 1e-12 of KPM_C128).  Replaces rec_A_vec (jclsquant/recurrence_functions.py:114-143)
  * and the device rec_A (jclsquant/cuda_cython/cuda/recursions.cu:267-317).
  */
 int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const double* v,
@@ -153,7 +155,8 @@ int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const 
  * P(H) = sum_{m<M} c[m] T_m(H) (c: the time-step moments of exp(-i H dt)),
  * steps >= 0 (0 copies v).  c: device [M] c128; v, out: device [R][n] c128; out
  * may alias v.  The R vectors advance together, one pass over H per order.
- * dtype KPM_C64 carries the vectors in complex64 between steps.
+ * dtype KPM_C64 carries the vectors in complex64 between steps, KPM_C128F in float
+ * pairs (~48 significant bits; the result is within 1e-12 of KPM_C128).
  * Replaces for_time (jclsquant/cuda_cython/cuda/obv.cu:93-122), which advances
  * U and U_c (R = 2) by len_t calls of the device rec_A each.
  */

@@ -103,65 +103,94 @@ struct HoneyDisp {
 };
 
 // Neighbour k (0..2) of site i: its column, or -1 where an open edge has no bond.
-__device__ inline int64_t honey_neighbour(int64_t i, int k, int nx, int ny, int periodic) {
-  const int64_t cell = i >> 1;
+// I is the index type: 32-bit arithmetic when every slot index fits (integer division
+// by nx and L is the costliest part of this kernel), 64-bit otherwise.
+template <typename I>
+__device__ inline I honey_neighbour(I i, int k, int nx, int ny, int periodic) {
+  const I cell = i >> 1;
   const int b = (int)(i & 1);
-  const int ix = (int)(cell % nx), iy = (int)(cell / nx);
+  const int iy = (int)(cell / (I)nx);
+  const int ix = (int)(cell - (I)iy * nx);
   const int sgn = b ? 1 : -1;  // B: +1 neighbours, A: -1
   const int xk = k == 1 ? ix + sgn : ix;
   const int yk = k == 2 ? iy + sgn : iy;
-  if (!periodic && (xk < 0 || xk >= nx || yk < 0 || yk >= ny)) return -1;
-  const int x = (xk % nx + nx) % nx;
-  const int y = (yk % ny + ny) % ny;
-  return 2 * ((int64_t)y * nx + x) + (1 - b);
+  if (!periodic && (xk < 0 || xk >= nx || yk < 0 || yk >= ny)) return (I)-1;
+  // a neighbour is at most one cell away: wrap by one period
+  const int x = xk < 0 ? xk + nx : (xk >= nx ? xk - nx : xk);
+  const int y = yk < 0 ? yk + ny : (yk >= ny ? yk - ny : yk);
+  return 2 * ((I)y * nx + x) + (1 - b);
 }
 
-// One thread per output slot t = i * L + s, so consecutive threads write consecutive
-// slots of every array.
-__global__ void honeycomb_kernel(int nx, int ny, int periodic, double t, const double* __restrict__ eps, int L,
+// One slot q = i * L + s: its value, column, valid flag, displacements and reverse-bond
+// slot.  e is the site's on-site energy (read only for the on-site slot).
+template <typename I, int L>
+__device__ inline void honey_slot(I q, double e, int nx, int ny, int periodic, double t, const HoneyDisp& d,
+                                  double2* data, int32_t* indices, int32_t* valid, double2* dxv, double2* dyv,
+                                  int64_t* partner) {
+  constexpr int first = L - 3;
+  const double2 zero = make_double2(0.0, 0.0);
+  const I i = q / (I)L;
+  const int s = (int)(q - i * L);
+  const int b = (int)(i & 1);
+  if (s < first) {  // on-site slot
+    data[q] = make_double2(e, 0.0);
+    indices[q] = (int32_t)i;
+    if (valid) valid[q] = 1;
+    if (dxv) dxv[q] = zero;
+    if (dyv) dyv[q] = zero;
+    if (partner) partner[q] = -1;
+    return;
+  }
+  const int k = s - first;
+  const I j = honey_neighbour<I>(i, k, nx, ny, periodic);
+  if (j >= 0) {
+    data[q] = make_double2(t, 0.0);
+    indices[q] = (int32_t)j;
+    if (valid) valid[q] = 1;
+    if (dxv) dxv[q] = make_double2(b ? d.bx[k] : d.ax[k], 0.0);
+    if (dyv) dyv[q] = make_double2(b ? d.by[k] : d.ay[k], 0.0);
+    if (partner) partner[q] = (int64_t)j * L + s;
+  } else {
+    // padding: the column of the last earlier bond of the row, else the row itself
+    I prev = i;
+    for (int kk = k - 1; kk >= 0; --kk) {
+      const I jj = honey_neighbour<I>(i, kk, nx, ny, periodic);
+      if (jj >= 0) {
+        prev = jj;
+        break;
+      }
+    }
+    data[q] = zero;
+    indices[q] = (int32_t)prev;
+    if (valid) valid[q] = 0;
+    if (dxv) dxv[q] = zero;
+    if (dyv) dyv[q] = zero;
+    if (partner) partner[q] = -1;
+  }
+}
+
+// One thread per output slot, so consecutive threads write consecutive slots of every
+// array.  Each thread takes kHoneyUnroll slots a grid stride apart and issues their
+// on-site loads before any store, so the loads' latency overlaps.
+constexpr int kHoneyUnroll = 4;
+
+template <typename I, int L>
+__global__ void honeycomb_kernel(int nx, int ny, int periodic, double t, const double* __restrict__ eps,
                                  HoneyDisp d, double2* data, int32_t* indices, int32_t* valid, double2* dxv,
                                  double2* dyv, int64_t* partner) {
-  const int64_t total = 2 * (int64_t)nx * ny * L;
-  const int first = L - 3;
-  const double2 zero = make_double2(0.0, 0.0);
-  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = q / L;
-    const int s = (int)(q - i * L);
-    const int b = (int)(i & 1);
-    if (s < first) {  // on-site slot
-      data[q] = make_double2(eps[i], 0.0);
-      indices[q] = (int32_t)i;
-      if (valid) valid[q] = 1;
-      if (dxv) dxv[q] = zero;
-      if (dyv) dyv[q] = zero;
-      if (partner) partner[q] = -1;
-      continue;
+  const I total = (I)2 * nx * ny * L;
+  const I stride = (I)gridDim.x * blockDim.x;
+  for (I q0 = (I)blockIdx.x * blockDim.x + threadIdx.x; q0 < total; q0 += kHoneyUnroll * stride) {
+    double e[kHoneyUnroll];
+#pragma unroll
+    for (int u = 0; u < kHoneyUnroll; ++u) {
+      const I q = q0 + u * stride;
+      e[u] = (L == 4 && q < total) ? __ldg(eps + q / (I)L) : 0.0;
     }
-    const int k = s - first;
-    const int64_t j = honey_neighbour(i, k, nx, ny, periodic);
-    if (j >= 0) {
-      data[q] = make_double2(t, 0.0);
-      indices[q] = (int32_t)j;
-      if (valid) valid[q] = 1;
-      if (dxv) dxv[q] = make_double2(b ? d.bx[k] : d.ax[k], 0.0);
-      if (dyv) dyv[q] = make_double2(b ? d.by[k] : d.ay[k], 0.0);
-      if (partner) partner[q] = j * L + s;
-    } else {
-      // padding: the column of the last earlier bond of the row, else the row itself
-      int64_t prev = i;
-      for (int kk = k - 1; kk >= 0; --kk) {
-        const int64_t jj = honey_neighbour(i, kk, nx, ny, periodic);
-        if (jj >= 0) {
-          prev = jj;
-          break;
-        }
-      }
-      data[q] = zero;
-      indices[q] = (int32_t)prev;
-      if (valid) valid[q] = 0;
-      if (dxv) dxv[q] = zero;
-      if (dyv) dyv[q] = zero;
-      if (partner) partner[q] = -1;
+#pragma unroll
+    for (int u = 0; u < kHoneyUnroll; ++u) {
+      const I q = q0 + u * stride;
+      if (q < total) honey_slot<I, L>(q, e[u], nx, ny, periodic, t, d, data, indices, valid, dxv, dyv, partner);
     }
   }
 }
@@ -317,10 +346,24 @@ int kpm_honeycomb_ell(int nx, int ny, int periodic, double t, const double* onsi
   }
   cudaStream_t s = stream_of(stream);
   const int64_t n = 2 * (int64_t)nx * ny;
-  honeycomb_kernel<<<stream_grid(n * len_row), kBlock, 0, s>>>(nx, ny, periodic, t, onsite, len_row, d,
-                                                      reinterpret_cast<double2*>(data), indices, valid,
-                                                      reinterpret_cast<double2*>(dx), reinterpret_cast<double2*>(dy),
-                                                      partner);
+  const int grid = stream_grid(n * len_row);
+  // 32-bit slot indices when they cannot overflow (unrolled grid-stride increments included)
+  const bool narrow = n * len_row + (int64_t)kHoneyUnroll * grid * kBlock < (int64_t)INT32_MAX;
+  double2* dd = reinterpret_cast<double2*>(data);
+  double2* dxx = reinterpret_cast<double2*>(dx);
+  double2* dyy = reinterpret_cast<double2*>(dy);
+  if (narrow && len_row == 4)
+    honeycomb_kernel<int32_t, 4><<<grid, kBlock, 0, s>>>(nx, ny, periodic, t, onsite, d, dd, indices, valid, dxx,
+                                                         dyy, partner);
+  else if (narrow)
+    honeycomb_kernel<int32_t, 3><<<grid, kBlock, 0, s>>>(nx, ny, periodic, t, onsite, d, dd, indices, valid, dxx,
+                                                         dyy, partner);
+  else if (len_row == 4)
+    honeycomb_kernel<int64_t, 4><<<grid, kBlock, 0, s>>>(nx, ny, periodic, t, onsite, d, dd, indices, valid, dxx,
+                                                         dyy, partner);
+  else
+    honeycomb_kernel<int64_t, 3><<<grid, kBlock, 0, s>>>(nx, ny, periodic, t, onsite, d, dd, indices, valid, dxx,
+                                                         dyy, partner);
   return check_cuda(cudaGetLastError());
 }
 

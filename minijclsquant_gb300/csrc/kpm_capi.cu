@@ -839,6 +839,14 @@ int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r, con
 int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const double* v, double* out,
                     void* stream) {
   if (!h || !c || !v || !out || R < 1 || M < 2) return KPM_ERR_INVALID_ARG;
+  if (dtype == KPM_C128F) {  // float-float complex128
+    for (int r0 = 0; r0 < R;) {
+      const int Rg = pow2_group(R - r0);
+      KPM_TRY(series_group_ff(h, R, r0, Rg, M, c, 1, v, out, as_stream(stream)));
+      r0 += Rg;
+    }
+    return KPM_OK;
+  }
   KPM_TRY(check_dtype(dtype));
   const bool f32 = dtype == KPM_C64;
   cudaStream_t s = as_stream(stream);
@@ -859,6 +867,14 @@ int kpm_cheb_series(kpm_ell* h, int dtype, int R, int M, const double* c, const 
 int kpm_time_evolve(kpm_ell* h, int dtype, int R, int M, const double* c, int steps, const double* v, double* out,
                     void* stream) {
   if (!h || !c || !v || !out || R < 1 || M < 2 || steps < 0) return KPM_ERR_INVALID_ARG;
+  if (dtype == KPM_C128F) {  // float-float complex128: the state stays in float pairs between steps
+    for (int r0 = 0; r0 < R;) {
+      const int Rg = pow2_group(R - r0);
+      KPM_TRY(series_group_ff(h, R, r0, Rg, M, c, steps, v, out, as_stream(stream)));
+      r0 += Rg;
+    }
+    return KPM_OK;
+  }
   KPM_TRY(check_dtype(dtype));
   const bool f32 = dtype == KPM_C64;
   cudaStream_t s = as_stream(stream);

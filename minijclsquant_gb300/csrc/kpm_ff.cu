@@ -19,6 +19,9 @@
 // Kernels: the first step (T_1 = H T_0, mu_0, mu_1) grid-stride, the later steps
 // with the bulk-copy stages and producer warp of the staged step kernels.  Each
 // thread serves one complex of one vector (R threads per row).
+#include <cstdlib>
+#include <string>
+
 #include "kpm_ff.cuh"
 #include "kpm_ws.cuh"
 
@@ -26,10 +29,26 @@ namespace kpm {
 
 namespace {
 
+// The series coefficient c_m as a complex float pair {re_hi, im_hi, re_lo, im_lo}.
+__device__ __forceinline__ float4 ff_coef(const double2* coef, int m) {
+  const double2 c = coef[m];
+  const float rh = (float)c.x, ih = (float)c.y;
+  return make_float4(rh, ih, (float)(c.x - (double)rh), (float)(c.y - (double)ih));
+}
+
+// series tile update o += c x (complex float pairs), normalised
+__device__ __forceinline__ void ff_series_add(FF& o, float4 c, const FF& x) {
+  ff_mac(o, c, x);
+  ff_norm(o.rh, o.rl);
+  ff_norm(o.ih, o.il);
+}
+
 // Grid-stride step.  FIRST: T_1 = (1/2)(2H) T_0 and the moments of T_0 and T_1,
 // partials [2 steps][grid][R].  NEXT (operators too wide for the staged stages):
 // T_{m+1} = 2H T_m - T_{m-1} in place and <v_l|T_{m+1}>, partials [grid][R].
-template <bool REAL, int R, bool NEXT>
+// SER (the series of rec_A_vec): no moments; FIRST writes series = c_0 T_0 + c_1 T_1,
+// NEXT adds c_m T_{m+1} to it.
+template <bool REAL, int R, bool NEXT, bool SER>
 __global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
   using MV = typename FFVal<REAL>::type;
   constexpr int RPB = kBlock / R;
@@ -39,9 +58,15 @@ __global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
   const float4* __restrict__ tcur = static_cast<const float4*>(p.tcur);
   const float4* __restrict__ vl = static_cast<const float4*>(p.vl);
   float4* tout = static_cast<float4*>(p.tout);
+  float4* series = static_cast<float4*>(p.series);
   double zr[1] = {0.0}, zi[1] = {0.0}, mr[1] = {0.0}, mi[1] = {0.0};
   FFMom z{0.f, 0.f, 0.f, 0.f}, m{0.f, 0.f, 0.f, 0.f};
   int pending = 0;
+  float4 c_lo = make_float4(0.f, 0.f, 0.f, 0.f), c_hi = c_lo;
+  if (SER) {
+    c_hi = ff_coef(p.coef, p.m);
+    if (!NEXT) c_lo = ff_coef(p.coef, 0);
+  }
   for (int64_t row = (int64_t)blockIdx.x * RPB + rl; row < p.n_pad; row += (int64_t)gridDim.x * RPB) {
     const int64_t vi = row * R + sub;
     FF acc{0.f, 0.f, 0.f, 0.f};
@@ -58,6 +83,14 @@ __global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
     ff_norm(acc.ih, acc.il);
     if (!NEXT) acc = FF{0.5f * acc.rh, 0.5f * acc.ih, 0.5f * acc.rl, 0.5f * acc.il};  // exact
     tout[vi] = ff_raw(acc);
+    if (SER) {
+      FF o{0.f, 0.f, 0.f, 0.f};
+      if (NEXT) o = ff_of(series[vi]);
+      else ff_series_add(o, c_lo, ff_of(__ldg(tcur + vi)));
+      ff_series_add(o, c_hi, acc);
+      series[vi] = ff_raw(o);
+      continue;
+    }
     const FF l = ff_of(__ldg(vl + vi));
     if (!NEXT) ff_cdot(z, l, ff_of(__ldg(tcur + vi)));
     ff_cdot(m, l, acc);
@@ -67,6 +100,7 @@ __global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
       ff_fold(mr[0], mi[0], m);
     }
   }
+  if (SER) return;
   ff_fold(zr[0], zi[0], z);
   ff_fold(mr[0], mi[0], m);
   if (NEXT) {
@@ -79,7 +113,9 @@ __global__ void __launch_bounds__(kBlock) ff_step_kernel(const StepParams p) {
 
 // T_{m+1} = 2H T_m - T_{m-1} (in place over T_{m-1}) and <v_l|T_{m+1}> per CTA, with
 // the staged tiles, producer warp and full/empty barriers of cheb_next_ws_kernel.
-template <bool REAL, int R, int U>
+// SER: no moments; the producer stages the series tile in the left-vector slot and the
+// compute warps write series + c_m T_{m+1}.
+template <bool REAL, int R, int U, bool SER>
 __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 3 : 1)) ff_next_kernel(const StepParams p) {
   using MV = typename FFVal<REAL>::type;
   constexpr int RPB = kBlock / R;
@@ -118,7 +154,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 3 : 1)) ff_next_kernel(c
       tc.col = p.col;
       tc.val = static_cast<const unsigned char*>(p.val);
       tc.old = static_cast<const unsigned char*>(p.tout);
-      tc.vl = static_cast<const unsigned char*>(p.vl);
+      tc.vl = static_cast<const unsigned char*>(SER ? p.series : p.vl);
       tc.vl2 = nullptr;
       tc.ld = p.ld;
       tc.L = L;
@@ -148,6 +184,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 3 : 1)) ff_next_kernel(c
 
   const float4* __restrict__ tcur = static_cast<const float4*>(p.tcur);
   float4* tout = static_cast<float4*>(p.tout);
+  float4* series = static_cast<float4*>(p.series);
+  const float4 cm = SER ? ff_coef(p.coef, p.m) : make_float4(0.f, 0.f, 0.f, 0.f);
   const int sub = threadIdx.x % R, rl = threadIdx.x / R;
   double mr[1] = {0.0}, mi[1] = {0.0};
   FFMom mom{0.f, 0.f, 0.f, 0.f};
@@ -212,6 +250,11 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 3 : 1)) ff_next_kernel(c
 #pragma unroll
     for (int u = 0; u < U; ++u) {
       tout[(row0 + u * RPB + rl) * R + sub] = ff_raw(acc[u]);
+      if (SER) {
+        ff_series_add(l[u], cm, acc[u]);
+        series[(row0 + u * RPB + rl) * R + sub] = ff_raw(l[u]);
+        continue;
+      }
       ff_cdot(mom, l[u], acc[u]);
       if (++pending == kFfFlush) {
         pending = 0;
@@ -219,6 +262,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 3 : 1)) ff_next_kernel(c
       }
     }
   }
+  if (SER) return;
   ff_fold(mr[0], mi[0], mom);
   block_reduce_store<R, 1>(mr, mi, p.part + (int64_t)blockIdx.x * R, red, true);
 }
@@ -237,11 +281,22 @@ __global__ void ff_pack_kernel(const double2* __restrict__ src, int64_t n, int64
   }
 }
 
-template <bool REAL, int R, int U>
+// float pairs [n_pad][Rg] -> complex128 [R][n] for vectors r0 .. r0 + Rg (hi + lo in FP64)
+__global__ void ff_unpack_kernel(const float4* __restrict__ src, int64_t n, int Rg, int r0, double2* __restrict__ dst) {
+  const int64_t total = n * Rg;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(t / n);
+    const int64_t row = t - (int64_t)r * n;
+    const float4 q = src[row * Rg + r];
+    dst[(int64_t)(r0 + r) * n + row] = make_double2((double)q.x + (double)q.z, (double)q.y + (double)q.w);
+  }
+}
+
+template <bool REAL, int R, int U, bool SER>
 bool ff_smem_attr(size_t smem) {
   static size_t configured = 0;
   if (smem <= configured) return true;
-  if (cudaFuncSetAttribute(ff_next_kernel<REAL, R, U>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+  if (cudaFuncSetAttribute(ff_next_kernel<REAL, R, U, SER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess) {
     (void)cudaGetLastError();
     return false;
@@ -258,32 +313,38 @@ size_t ff_stage_bytes(int L) {
 }
 
 // One launch: kind -1 the first step, 0 a grid-stride later step, 1 / 2 a staged
-// later step with U = kind rows per thread.
-template <bool REAL, int R, int U>
+// later step with U = kind rows per thread.  A series step (p.series set) runs the
+// SER instantiations.
+template <bool REAL, int R, int U, bool SER>
 int ff_launch_staged(const StepParams& p, int grid, cudaStream_t s) {
   const size_t smem = kWsStages * ff_stage_bytes<REAL, R, U>(p.L);
-  if (!ff_smem_attr<REAL, R, U>(smem)) return KPM_ERR_UNSUPPORTED;
-  ff_next_kernel<REAL, R, U><<<grid, kWsThreads, smem, s>>>(p);
+  if (!ff_smem_attr<REAL, R, U, SER>(smem)) return KPM_ERR_UNSUPPORTED;
+  ff_next_kernel<REAL, R, U, SER><<<grid, kWsThreads, smem, s>>>(p);
+  return check_cuda(cudaGetLastError());
+}
+
+template <bool REAL, int R, bool SER>
+int ff_launch_ser(int kind, const StepParams& p, int grid, cudaStream_t s) {
+  if (kind < 0)
+    ff_step_kernel<REAL, R, false, SER><<<grid, kBlock, 0, s>>>(p);
+  else if (kind == 0)
+    ff_step_kernel<REAL, R, true, SER><<<grid, kBlock, 0, s>>>(p);
+  else
+    return kind == 2 ? ff_launch_staged<REAL, R, 2, SER>(p, grid, s) : ff_launch_staged<REAL, R, 1, SER>(p, grid, s);
   return check_cuda(cudaGetLastError());
 }
 
 template <bool REAL, int R>
 int ff_launch(int kind, const StepParams& p, int grid, cudaStream_t s) {
-  if (kind < 0)
-    ff_step_kernel<REAL, R, false><<<grid, kBlock, 0, s>>>(p);
-  else if (kind == 0)
-    ff_step_kernel<REAL, R, true><<<grid, kBlock, 0, s>>>(p);
-  else
-    return kind == 2 ? ff_launch_staged<REAL, R, 2>(p, grid, s) : ff_launch_staged<REAL, R, 1>(p, grid, s);
-  return check_cuda(cudaGetLastError());
+  return p.series ? ff_launch_ser<REAL, R, true>(kind, p, grid, s) : ff_launch_ser<REAL, R, false>(kind, p, grid, s);
 }
 
 template <bool REAL, int R, int U>
 int ff_ctas(int L) {
   const size_t smem = kWsStages * ff_stage_bytes<REAL, R, U>(L);
-  if (smem > 200 * 1024 || !ff_smem_attr<REAL, R, U>(smem)) return 0;
+  if (smem > 200 * 1024 || !ff_smem_attr<REAL, R, U, false>(smem)) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ff_next_kernel<REAL, R, U>, kWsThreads, smem) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ff_next_kernel<REAL, R, U, false>, kWsThreads, smem) !=
       cudaSuccess) {
     (void)cudaGetLastError();
     return 0;
@@ -318,22 +379,29 @@ int ff_occupancy(bool real, int R, int U, int L) {
 #undef KPM_FO
 }
 
-// The later-step kernel for (operator, R): the grid-stride kernel or the staged
-// kernel with 1 or 2 rows per thread, timed on the operator (a few launches on
-// zeroed vectors) and kept in the handle's tuned list (key 2000 + 10 R).
-int ff_config(kpm_ell_s* h, int Rg, cudaStream_t s, StepConfig* out) {
-  const int key = 2000 + Rg * 10;
+// The later-step kernel for (operator, R, series step or moment step): the grid-stride
+// kernel or the staged kernel with 1 or 2 rows per thread, timed on the operator (a few
+// launches on zeroed vectors) and kept in the handle's tuned list (key 2000 + 10 R, + 1
+// for series steps).  KPM_STEP_KERNEL=simple|ws1|ws2 forces one.  Timing clears ws.ta,
+// ws.tb and ws.vl: callers tune before they fill those.
+int ff_config(kpm_ell_s* h, int Rg, bool series, cudaStream_t s, StepConfig* out) {
+  const int key = 2000 + Rg * 10 + (series ? 1 : 0);
   for (auto& kv : h->tuned)
     if (kv.first == key) {
       *out = kv.second;
       return KPM_OK;
     }
+  const char* force = getenv("KPM_STEP_KERNEL");
+  const std::string f = force ? force : "";
   std::vector<StepConfig> cands;
-  StepConfig c0;
-  c0.kind = 0;
-  c0.grid = grid_for(h, Rg, 1);
-  cands.push_back(c0);
+  if (f.empty() || f == "simple") {
+    StepConfig c0;
+    c0.kind = 0;
+    c0.grid = grid_for(h, Rg, 1);
+    cands.push_back(c0);
+  }
   for (int U = 1; U <= 2; ++U) {
+    if (!f.empty() && f != std::string("ws") + (U == 1 ? "1" : "2")) continue;
     const int occ = ff_occupancy(h->is_real != 0, Rg, U, h->L);
     if (occ <= 0) continue;
     const int64_t ntiles = h->n_pad / ((kBlock / Rg) * U);
@@ -342,6 +410,12 @@ int ff_config(kpm_ell_s* h, int Rg, cudaStream_t s, StepConfig* out) {
     c.U = U;
     c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
     cands.push_back(c);
+  }
+  if (cands.empty()) {  // a forced form that cannot serve this operator
+    StepConfig c0;
+    c0.kind = 0;
+    c0.grid = grid_for(h, Rg, 1);
+    cands.push_back(c0);
   }
   if (cands.size() > 1) {
     int max_grid = 0;
@@ -355,11 +429,18 @@ int ff_config(kpm_ell_s* h, int Rg, cudaStream_t s, StepConfig* out) {
     KPM_CUDA_TRY(cudaMemsetAsync(ws.ta.p, 0, vb, s));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.tb.p, 0, vb, s));
     KPM_CUDA_TRY(cudaMemsetAsync(ws.vl.p, 0, vb, s));
+    KPM_CUDA_TRY(cudaMemsetAsync(ws.part.p, 0, sizeof(double2), s));
     StepParams p = base_params(h, true);
     p.tcur = ws.ta.p;
     p.tout = ws.tb.p;
-    p.vl = ws.vl.p;
     p.part = static_cast<double2*>(ws.part.p);
+    if (series) {  // series into ws.vl with a zero coefficient
+      p.series = ws.vl.p;
+      p.coef = static_cast<const double2*>(ws.part.p);
+      p.m = 0;
+    } else {
+      p.vl = ws.vl.p;
+    }
     cudaEvent_t e0, e1;
     KPM_CUDA_TRY(cudaEventCreate(&e0));
     KPM_CUDA_TRY(cudaEventCreate(&e1));
@@ -385,7 +466,70 @@ int ff_config(kpm_ell_s* h, int Rg, cudaStream_t s, StepConfig* out) {
   return KPM_OK;
 }
 
+int ff_pack(const double* v, int64_t n, int64_t n_pad, int R, int r0, int Rg, void* dst, cudaStream_t s) {
+  const int64_t total = n_pad * Rg;
+  const int pg = (int)std::min<int64_t>((total + 255) / 256, 65536);
+  ff_pack_kernel<<<pg, 256, 0, s>>>(reinterpret_cast<const double2*>(v), n, n_pad, R, r0, Rg,
+                                    static_cast<float4*>(dst));
+  return check_cuda(cudaGetLastError());
+}
+
+// sum_{m<M} c_m T_m x for one packed float-pair set x (ws.ta / ws.tb carry the recursion)
+int ff_series_packed(kpm_ell_s* h, int Rg, int M, const StepConfig& cfg, const double2* coef, const void* x,
+                     void* result, cudaStream_t s) {
+  const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_CUDA_TRY(cudaMemcpyAsync(ws.ta.p, x, vb, cudaMemcpyDeviceToDevice, s));
+  StepParams p = base_params(h, true);
+  p.series = result;
+  p.coef = coef;
+  p.tcur = ws.ta.p;
+  p.tout = ws.tb.p;
+  p.m = 1;
+  KPM_TRY(ff_dispatch(h->is_real != 0, Rg, -1, p, grid_for(h, Rg, 1), s));
+  void* tprev = ws.ta.p;
+  void* tcur = ws.tb.p;
+  cudaEvent_t ev = nullptr;
+  if (M > 2) KPM_TRY(prof_begin(h, s, &ev));
+  for (int m = 2; m < M; ++m) {
+    p.tcur = tcur;
+    p.tout = tprev;
+    p.m = m;
+    KPM_TRY(ff_dispatch(h->is_real != 0, Rg, cfg.kind == 0 ? 0 : cfg.U, p, cfg.grid, s));
+    std::swap(tprev, tcur);
+  }
+  if (M > 2) KPM_TRY(prof_end(h, s, ev, M - 2));
+  return KPM_OK;
+}
+
 }  // namespace
+
+// out[r] = P^steps v[r], P = sum_{m<M} c_m T_m(H), for vectors r0 .. r0 + Rg in float-float
+// arithmetic (steps = 1: the series of rec_A_vec).  The state ping-pongs between ws.tc and
+// ws.acc; the recursion uses ws.ta / ws.tb.
+int series_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* c, int steps, const double* v,
+                    double* out, cudaStream_t s) {
+  KPM_TRY(ensure_f32_values(h, s));
+  StepConfig cfg;
+  if (M > 2) KPM_TRY(ff_config(h, Rg, true, s, &cfg));
+  const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.tc, vb));
+  KPM_TRY(ensure(ws.acc, vb));
+  KPM_TRY(ff_pack(v, h->n, h->n_pad, R, r0, Rg, ws.tc.p, s));
+  void* x = ws.tc.p;
+  void* y = ws.acc.p;
+  for (int j = 0; j < steps; ++j) {
+    KPM_TRY(ff_series_packed(h, Rg, M, cfg, reinterpret_cast<const double2*>(c), x, y, s));
+    std::swap(x, y);
+  }
+  const int64_t total = h->n * Rg;
+  const int g = (int)std::min<int64_t>((total + 255) / 256, 65536);
+  ff_unpack_kernel<<<g, 256, 0, s>>>(static_cast<const float4*>(x), h->n, Rg, r0, reinterpret_cast<double2*>(out));
+  return check_cuda(cudaGetLastError());
+}
 
 // DOS / two-vector moments <v_l|T_m v_r> of one group of Rg vectors in float-float arithmetic.
 int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v_r, const double* v_l, double* mu,
@@ -397,7 +541,7 @@ int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v
   KPM_TRY(ensure(ws.tb, vb));
   KPM_TRY(ensure(ws.vl, vb));
   StepConfig cfg;
-  KPM_TRY(ff_config(h, Rg, s, &cfg));
+  KPM_TRY(ff_config(h, Rg, false, s, &cfg));
   const int grid_first = grid_for(h, Rg, 1);
   const int grid_next = cfg.grid;
   const int grid = std::max(grid_next, grid_first);

@@ -185,6 +185,9 @@ int check_dtype(int dtype);
 // KPM_C128F: moments of one vector group in float-float arithmetic (kpm_ff.cu).
 int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v_r, const double* v_l, double* mu,
                      cudaStream_t s);
+// KPM_C128F: out = (sum_{m<M} c_m T_m)^steps v for one vector group (kpm_ff.cu).
+int series_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* c, int steps, const double* v,
+                    double* out, cudaStream_t s);
 
 // Rows per tile of the staged kernel (complex64 packs two vectors per thread).
 inline int staged_tile_rows(bool f32, int R, int U) {

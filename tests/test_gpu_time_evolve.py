@@ -209,3 +209,71 @@ def test_series_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, 
         assert _rel(s[r], ref) <= tol, (kernel, r, _rel(s[r], ref))
         ref2 = oracle.rec_A_vec(M, Hk.data, Hk.indices, Hk.len_row, c, ref)
         assert _rel(e[r], ref2) <= tol, (kernel, r, _rel(e[r], ref2))
+
+
+@pytest.mark.parametrize("complex_op", [False, True])
+@pytest.mark.parametrize("kernel", ["simple", "ws1", "ws2"])
+@pytest.mark.parametrize("R", [1, 2, 8])
+def test_series_float_float_every_kernel(cuda_lib, monkeypatch, kernel, R, complex_op):
+    """KPM_C128F series and time evolution (float-float arithmetic on the FP32 pipe) on each
+    float-float step kernel, forced, against the oracle at the complex128 tolerance."""
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.kernel_and_moments import moments_U
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    monkeypatch.setenv("KPM_STEP_KERNEL", kernel)
+    if complex_op:
+        Hk = _complex_lattice(40, 36, 8)
+    else:
+        Hk = lattice.honeycomb(40, 36, t=-2.7, W=0.7, seed=5).modifier(modifier_bounds)
+    op = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row)
+    M = 60
+    c = moments_U(4.0, M).astype(np.complex128)
+    vs = np.stack([random_vector_generator(op.n, 500 + r) for r in range(R)])
+    s = device.cheb_series(op, M, c, vs, dtype="c128f")
+    e = device.time_evolve(op, M, c, 3, vs, dtype="c128f")
+    assert cuda_lib.kpm_ell_check(op.handle, None) == 0
+    for r in range(R):
+        ref = oracle.rec_A_vec(M, Hk.data, Hk.indices, Hk.len_row, c, vs[r])
+        assert _rel(s[r], ref) <= REL, (kernel, r, _rel(s[r], ref))
+        for _ in range(2):
+            ref = oracle.rec_A_vec(M, Hk.data, Hk.indices, Hk.len_row, c, ref)
+        assert _rel(e[r], ref) <= REL, (kernel, r, _rel(e[r], ref))
+
+
+def test_time_evolve_float_float_matches_reference_golden(cuda_lib):
+    from minijclsquant_gb300 import device
+
+    z = golden("time_evolution_6x5")
+    op = device.DeviceELL(z["data_kpm"], z["indices"], int(z["len_row"]))
+    out = device.time_evolve(op, int(z["M"]), z["c"], int(z["len_t"]), np.stack([z["U0"], z["Uc0"]]),
+                             dtype="c128f")
+    assert _rel(out[0], z["U"]) <= REL
+    assert _rel(out[1], z["Uc"]) <= REL
+    x = golden("honeycomb_8x8_more")
+    h8 = golden("honeycomb_8x8")
+    op8 = device.DeviceELL(h8["data_kpm"], h8["indices"], int(h8["len_row"]))
+    s = device.cheb_series(op8, len(x["coef"]), x["coef"], h8["v"][0], dtype="c128f")
+    assert _rel(s, x["series"]) <= REL
+
+
+def test_time_evolve_float_float_full_size_against_complex128(cuda_lib):
+    import torch
+
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.kernel_and_moments import moments_U
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    H = lattice.honeycomb(512, 512, t=-2.7, W=1.0, seed=3)
+    Hk = H.modifier(modifier_bounds)
+    op = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row)
+    M = 64
+    c = moments_U(3.0, M).astype(np.complex128)
+    v = torch.from_numpy(np.stack([random_vector_generator(op.n, 5 + r) for r in range(2)])).cuda()
+    f = device.time_evolve(op, M, c, 5, v, dtype="c128f")
+    d = device.time_evolve(op, M, c, 5, v)
+    assert float(torch.max(torch.abs(f - d)) / torch.max(torch.abs(d))) <= 1e-12
+    n0 = torch.linalg.vector_norm(v, dim=1)
+    assert float(torch.max(torch.abs(torch.linalg.vector_norm(f, dim=1) - n0) / n0)) <= 1e-10

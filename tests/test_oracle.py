@@ -1,13 +1,11 @@
 """The oracle (C restatement of jclsquant's CPU path) pinned against the
 golden vectors produced by the reference itself (tests/golden/make_golden.py).
 CPU only."""
-import os
-
 import numpy as np
 import pytest
 
 from conftest import golden
-from oracle import oracle
+from oracle import oracle, reference_import
 
 CASES = ["honeycomb_8x8", "ref_graphene_256", "complex_open_6x5", "irregular_300"]
 
@@ -121,11 +119,9 @@ def test_oracle_adjoint_gradient_against_finite_differences():
         assert abs(g[q] - fd) <= 1e-7 * max(1.0, abs(fd)), (q, g[q], fd)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/jclsquant"), reason="reference tree not present")
+@pytest.mark.skipif(not reference_import.available(), reason="reference tree not present")
 def test_oracle_against_live_reference():
     """Fresh seeded case, run through the live reference (built from its .pyx) and the oracle."""
-    from oracle import reference_import
-
     ref = reference_import.load()
     from minijclsquant_gb300 import lattice
 
@@ -141,3 +137,22 @@ def test_oracle_against_live_reference():
     ref.blas_funs.aAxby(2 + 0j, -1 + 0j, v, y_ref, Hk.data, Hk.indices, H.len_row, H.shape[0], 2)
     oracle.aAxby(2, -1, v, y, Hk.data, Hk.indices, H.len_row)
     assert np.max(np.abs(y - y_ref)) <= 1e-14 * np.max(np.abs(y_ref))
+
+
+def test_oracle_known_answers():
+    """The oracle on operators with closed-form moments: diag(e) gives
+    sum_i |v_i|^2 cos(m arccos e_i); the periodic chain (S + S^dagger)/2 gives
+    (1/2) sum_i conj(v_i)(v_{i+m} + v_{i-m})."""
+    rng = np.random.default_rng(5)
+    n, M = 2000, 200
+    e = rng.uniform(-0.99, 0.99, n)
+    v = np.exp(2j * np.pi * rng.random(n))
+    mu = oracle.rec_A_tab(M, e.astype(np.complex128), np.arange(n, dtype=np.int32), 1, v)
+    ref = np.array([np.sum(np.abs(v) ** 2 * np.cos(m * np.arccos(e))) for m in range(M)])
+    assert oracle.moment_tolerance_ok(mu, ref, 1e-10)[0]
+    i = np.arange(n)
+    idx = np.stack([(i + 1) % n, (i - 1) % n], axis=1).astype(np.int32).reshape(-1)
+    mu = oracle.rec_A_tab(M, np.full(2 * n, 0.5, dtype=np.complex128), idx, 2, v)
+    ref = np.array([0.5 * np.vdot(v, np.roll(v, -m) + np.roll(v, m)) for m in range(M)])
+    assert oracle.moment_tolerance_ok(mu, ref, 1e-10)[0]
+    assert abs(mu[0] - n) <= 1e-12 * n

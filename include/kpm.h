@@ -217,6 +217,9 @@ int kpm_adjoint_backward_ex(kpm_ell* h, const double* c, double* grad, int dtype
  *   vectors (the workspace holds 2 x 256 rows of 2 x group x n floats: 34 GB
  *   at n = 2.1M, group 4); the contraction runs on tcgen05 tensor cores (kind::tf32, 3xTF32 split, FP32 accumulation, split-K
  *   reduced in FP64).  v: device [R][n] c128; mu: device [Nm][Nm] c128.
+ *   When V holds complex values on H's ELL columns (checked on the device once per
+ *   pair of handles), V T_m is formed inside the H recursion step from the same
+ *   gathers of T_m (KPM_MU_NM_UNFUSED=1 in the environment keeps them separate).
  * kpm_mu_contract: the contraction alone, mu (+)= scale * sum_k conj(L_n) R_m
  *   for row blocks L, R of 256 complex64 vectors ([256][ld] floats, interleaved
  *   re/im, rows >= Nm ignored), k_floats = 2 * vector length (multiple of 16),

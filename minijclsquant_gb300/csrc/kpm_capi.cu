@@ -2,6 +2,7 @@
 // recursion drivers (moments, series, commutator, time-domain Kubo) and the
 // reference-compatible host-pointer entry points.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -637,6 +638,8 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
   *out = nullptr;
   cudaStream_t s = as_stream(stream);
   kpm_ell_s* h = new kpm_ell_s();
+  static std::atomic<uint64_t> next_id{1};
+  h->id = next_id.fetch_add(1);
   h->n = n_rows;
   h->L = len_row;
   h->n_pad = ((n_rows + kRowAlign - 1) / kRowAlign) * kRowAlign;

@@ -108,6 +108,10 @@ struct kpm_ell_s {
   // H == H^dagger, checked on the device at creation; doubling allowed for DOS moments
   int hermitian = 0;
   int doubling = 0;  // requested (KPM_FLAG_DOUBLING / kpm_ell_set_doubling)
+  // process-unique id of this handle, and the id of an operator whose ELL column arrays
+  // were found equal to this one's (kpm_mu_nm fuses V T_m into the H step then)
+  uint64_t id = 0;
+  uint64_t same_cols_id = 0;
 };
 
 namespace kpm {
@@ -185,6 +189,11 @@ int check_dtype(int dtype);
 // KPM_C128F: moments of one vector group in float-float arithmetic (kpm_ff.cu).
 int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v_r, const double* v_l, double* mu,
                      cudaStream_t s);
+// Kubo right rows: T_{m+1} = 2H T_m - T_{m-1} and B_m = V T_m in one pass when V has H's
+// columns (kpm_kubo_step.cu); complex64, complex V values (float4 splits), R in {1, 2, 4}.
+// launch == false only checks that the form fits (KPM_ERR_UNSUPPORTED otherwise).
+int kubo_step(bool real_h, int R, const StepParams& p, const void* vval, void* bout, int sm_count, cudaStream_t s,
+              bool launch);
 // KPM_C128F: out = (sum_{m<M} c_m T_m)^steps v for one vector group (kpm_ff.cu).
 int series_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* c, int steps, const double* v,
                     double* out, cudaStream_t s);

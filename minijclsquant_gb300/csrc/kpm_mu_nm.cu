@@ -21,6 +21,7 @@
 // correlator of kpm_time_sigma); the operator conventions are those of
 // modifier_velocity (jclsquant/modifiers.py:56-79).
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "kpm_async.cuh"
@@ -375,6 +376,44 @@ int kpm_mu_contract(const float* L, const float* R, int64_t k_floats, int64_t ld
   return rc != KPM_OK ? rc : herr;
 }
 
+// Sets *flag when two [count] column arrays differ anywhere.
+__global__ void cols_differ_kernel(const int32_t* __restrict__ a, const int32_t* __restrict__ b, int64_t count,
+                                   unsigned* flag) {
+  unsigned d = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+    d |= (a[i] != b[i]) ? 1u : 0u;
+  if (__any_sync(0xffffffffu, d) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
+}
+
+// Whether V's ELL column arrays equal H's (checked on the device once per pair of handles).
+int same_columns(kpm_ell_s* h, kpm_ell_s* v, cudaStream_t s, bool* same) {
+  *same = false;
+  if (v->same_cols_id == h->id) {
+    *same = true;
+    return KPM_OK;
+  }
+  if (v->L != h->L || v->n_pad != h->n_pad) return KPM_OK;
+  DevBuf f;
+  KPM_TRY(ensure(f, sizeof(unsigned)));
+  unsigned host = 1;
+  const int64_t count = (int64_t)h->L * h->n_pad;
+  int st = check_cuda(cudaMemsetAsync(f.p, 0, sizeof(unsigned), s));
+  if (st == KPM_OK) {
+    cols_differ_kernel<<<(int)std::min<int64_t>((count + 255) / 256, 4096), 256, 0, s>>>(h->col, v->col, count,
+                                                                                        static_cast<unsigned*>(f.p));
+    st = check_cuda(cudaGetLastError());
+  }
+  if (st == KPM_OK) st = check_cuda(cudaMemcpyAsync(&host, f.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  if (st == KPM_OK) st = check_cuda(cudaStreamSynchronize(s));
+  release(f);
+  if (st != KPM_OK) return st;
+  if (host == 0) {
+    v->same_cols_id = h->id;
+    *same = true;
+  }
+  return KPM_OK;
+}
+
 int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double* mu, void* stream) {
   if (!h || !v_op || !v || !mu || R < 1 || Nm < 2 || Nm > 256) return KPM_ERR_INVALID_ARG;
   if (v_op->n != h->n) return KPM_ERR_SHAPE;
@@ -431,7 +470,8 @@ int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double*
       ph.tout = A + (size_t)(m + 1) * lda;
       KPM_TRY(next(ph));
     }
-    // T recursion on v (in place), B[m] = V T_m
+    // T recursion on v (in place), B[m] = V T_m; when V has H's columns (and complex
+    // values) the product rides in the H step: one gather of T_m for both operators
     void* t_prev = ws.ta.p;  // T_0
     void* t_cur = ws.tb.p;
     pv.tcur = t_prev;
@@ -441,7 +481,19 @@ int kpm_mu_nm(kpm_ell* h, kpm_ell* v_op, int R, int Nm, const double* v, double*
     pt.tcur = t_prev;
     pt.tout = t_cur;
     KPM_TRY(launch_step(true, h->is_real, Rg, MODE_FIRST, EPI_STORE, pt, grid_h, s));
+    bool fuse = false;
+    if (!v_op->is_real && !getenv("KPM_MU_NM_UNFUSED")) {
+      KPM_TRY(same_columns(h, v_op, s, &fuse));
+      if (fuse) fuse = kubo_step(h->is_real != 0, Rg, pt, v_op->val32, nullptr, h->sm_count, s, false) == KPM_OK;
+    }
     for (int m = 1; m < Nm; ++m) {
+      if (fuse && m + 1 < Nm) {
+        pt.tcur = t_cur;
+        pt.tout = t_prev;
+        KPM_TRY(kubo_step(h->is_real != 0, Rg, pt, v_op->val32, B + (size_t)m * lda, h->sm_count, s, true));
+        std::swap(t_prev, t_cur);
+        continue;
+      }
       pv.tcur = t_cur;
       pv.tout = B + (size_t)m * lda;
       KPM_TRY(launch_step(true, v_op->is_real, Rg, MODE_APPLY, EPI_STORE, pv, grid_v, s));

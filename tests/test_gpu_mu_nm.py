@@ -110,3 +110,48 @@ def test_mu_nm_matches_fp64_restatement(cuda_lib, Nm, R):
     ref = _oracle_mu_nm(Hk.data, Vk, Hk.indices, Hk.len_row, vs, Nm)
     err = np.max(np.abs(mu.cpu().numpy() - ref)) / np.max(np.abs(ref))
     assert err < 1e-4, err
+
+
+@pytest.mark.parametrize("R", [1, 2, 4, 5])
+def test_fused_velocity_step_matches_separate_products(cuda_lib, monkeypatch, R):
+    """V T_m computed inside the H step (V with H's columns) against the separate V product,
+    for every vector-group width; and a V with other columns takes the separate path."""
+    import torch
+
+    from minijclsquant_gb300 import _capi, device, lattice
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    H = lattice.honeycomb(40, 30, t=-2.7, W=1.0, seed=8)
+    Hk = H.modifier(modifier_bounds)
+    Vk = H.modifier(modifier_velocity, "y").data / H.bounds[1]
+    n = H.shape[0]
+    Nm = 96
+    vs = torch.from_numpy(np.stack([random_vector_generator(n, 70 + r) for r in range(R)])).cuda()
+
+    def run(unfused):
+        if unfused:
+            monkeypatch.setenv("KPM_MU_NM_UNFUSED", "1")
+        else:
+            monkeypatch.delenv("KPM_MU_NM_UNFUSED", raising=False)
+        hop = device.DeviceELL(Hk.data, Hk.indices, Hk.len_row)
+        vop = device.DeviceELL(Vk, Hk.indices, Hk.len_row)
+        mu = torch.empty((Nm, Nm), dtype=torch.complex128, device="cuda")
+        st = cuda_lib.kpm_mu_nm(hop.handle, vop.handle, R, Nm, vs.data_ptr(), mu.data_ptr(), None)
+        assert st == 0, _capi.lib().kpm_strerror(st)
+        assert cuda_lib.kpm_ell_check(hop.handle, None) == 0
+        return mu.cpu().numpy()
+
+    fused, separate = run(False), run(True)
+    assert np.max(np.abs(fused - separate)) <= 1e-6 * np.max(np.abs(separate))
+    # a velocity operator with its own (permuted) column order: same matrix, separate products
+    L = Hk.len_row
+    perm = np.arange(L)[::-1]
+    Vp = Vk.reshape(n, L)[:, perm].reshape(-1)
+    Ip = Hk.indices.reshape(n, L)[:, perm].reshape(-1)
+    hop = device.DeviceELL(Hk.data, Hk.indices, L)
+    vop = device.DeviceELL(Vp, Ip, L)
+    mu = torch.empty((Nm, Nm), dtype=torch.complex128, device="cuda")
+    monkeypatch.delenv("KPM_MU_NM_UNFUSED", raising=False)
+    assert cuda_lib.kpm_mu_nm(hop.handle, vop.handle, R, Nm, vs.data_ptr(), mu.data_ptr(), None) == 0
+    assert np.max(np.abs(mu.cpu().numpy() - separate)) <= 1e-5 * np.max(np.abs(separate))

@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--adj-fd", type=int, default=64, help="parameters checked by central differences")
     ap.add_argument("--no-setup", action="store_true", help="skip the operator-construction measurement")
     ap.add_argument("--no-sigma", action="store_true", help="skip the time-domain Kubo (for_time_sigma) measurement")
+    ap.add_argument("--no-driven", action="store_true", help="skip the light-pulse operator update measurement")
     ap.add_argument("--sigma-cells", type=int, default=1024)
     ap.add_argument("--sigma-M", type=int, default=512, help="Fermi-Dirac (commutator series) terms")
     ap.add_argument("--sigma-len-t", type=int, default=32)
@@ -441,6 +442,49 @@ def run_time_sigma(a, hbm_peak, world):
                                "sample": "for_time_sigma restated in C (oracle), len_t=%d, same lattice and M, M2 "
                                          "(%.2f s)" % (lt, dt)}
     del Hk, V1, V2
+    torch.cuda.empty_cache()
+    return blk
+
+
+def run_driven(a, hbm_peak):
+    """The operator of a light-driven system, H(t) = H0 o exp(i A0 (cos wt dx + sin wt dy) / ch)
+    (the circular pulse form of light_modifier_cython, Extra_funs.pyx:301-317), written into
+    the operator's values on the device once per time step (kpm_ell_light_update), on the DOS
+    lattice with its bond vectors.  Algorithmic bytes per slot: H0, dx, dy read and the
+    stored value written, 4 x 16 B."""
+    import torch
+
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    g = lattice.honeycomb_device(a.cells, a.cells, t=-2.7, W=a.W, seed=1234, geometry=True)
+    op = device.DeviceELL(g.data_kpm, g.indices, g.len_row, complex_values=True)
+    prm = (2.0, 1.7, "r", 0.8)
+    op.light_update(g.data_kpm, g.dx, g.dy, "circle_packed", prm, 0.5)  # warm-up
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    reps = 10
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(reps):
+        op.light_update(g.data_kpm, g.dx, g.dy, "circle_packed", prm, 0.5 + 0.01 * k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    # each update ends with the device Hermiticity check (one more pass over the values)
+    ms = e0.elapsed_time(e1) / reps
+    slots = float(g.n) * g.len_row
+    gbs = slots * 64 / (ms * 1e-3) / 1e9
+    herm = bool(op.hermitian)
+    v = torch.from_numpy(random_vector_generator(g.n, 3)).cuda()
+    mu = device.cheb_moments(op, 64, v)
+    blk = {"sites": g.n, "ms_per_update": ms, "hermitian_after_update": herm,
+           "mu0_over_n": float(abs(mu[0].item()) / g.n),
+           "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                        "kernel": "light_update_kernel + hermitian_check_kernel",
+                        "algorithmic_bytes_per_update": slots * 64},
+           "note": "kpm_ell_light_update: H(t) into the operator's stored values, once per time step"}
+    del op, g
     torch.cuda.empty_cache()
     return blk
 
@@ -1021,6 +1065,8 @@ def run_ours(a):
         line["setup"] = run_setup(a, prob, host_build_s, hbm_peak)
     if not a.no_sigma:
         line["time_sigma"] = run_time_sigma(a, hbm_peak, world)
+    if not a.no_driven:
+        line["driven"] = run_driven(a, hbm_peak)
     clocks = clk.summary()
     if clocks is not None:
         line["clocks"] = clocks

@@ -57,6 +57,9 @@ extern "C" {
 #define KPM_FLAG_DEVICE_PTRS 1u   /* data/indices are device pointers        */
 #define KPM_FLAG_SPLIT_DIAG 2u    /* accepted; the diagonal stays an ELL slot  */
 #define KPM_FLAG_DOUBLING 4u      /* DOS moments by the doubling identity      */
+#define KPM_FLAG_COMPLEX 8u       /* store complex values even when every imaginary
+                                     part is zero (an operator whose values will be
+                                     made complex later, e.g. kpm_ell_light_update) */
 
 typedef struct kpm_ell_s kpm_ell;
 
@@ -324,6 +327,36 @@ int kpm_honeycomb_ell(int nx, int ny, int periodic, double t, const double* onsi
 int kpm_ell_gershgorin_partner(int64_t n, int len_row, const double* data, const int32_t* indices,
                                const int64_t* partner, double factor, double* bound, void* stream);
 int kpm_ell_scale_values(int64_t count, double scale, double* data, void* stream);
+
+/* ---- time-dependent operators of driven systems ---------------------------
+ * Complex scalars are passed as host arrays of (re, im) pairs; arrays are device
+ * c128 in the reference's padded row-major ELL layout.
+ * kpm_light_modifier: the Peierls substitution of light_modifier_cython
+ *   (jclsquant/cython_modules/Extra_funs.pyx:236-342):
+ *     data_new[i] = a data[i] exp(i A0 (cx dx[i] + cy dy[i]) / ch),
+ *   (cx, cy) = (0, sin wt) if eta == 0 (linear) else (cos wt, eta sin wt) (circular),
+ *   ch = cosh((t - 2 Tp) / (0.5673 Tp)) if Tp != 0 (pulse), else 1.
+ *   params: [6] complex a, A0, t, w, Tp, eta.  data_new may alias data.
+ * kpm_ell_light_update: the same H(t) from H0 = data0 written straight into h's stored
+ *   values (one pass, no array in between; kpm_ell_set_values semantics afterwards).
+ *   h must store complex values: create it with KPM_FLAG_COMPLEX (KPM_ERR_DTYPE otherwise).
+ * kpm_phonon_modifier: hopping_pos_phonons_modifier (Extra_funs.pyx:540-560): for every
+ *   slot whose column is not its row, dx_new = dx + Aq (ex[row] cos(wq t - q0 Sx[row])
+ *   - ex[col] cos(wq t - q0 Sx[col])) / ch, dy_new likewise (ey, q1, Sy), data_new =
+ *   data exp(-b (sqrt(|dx_new|^2 + |dy_new|^2) / a0 - 1)), ch = cosh((t - 2 Tp) /
+ *   (0.5673 Tp)), Tp = 2 pi / wq; the other slots of the outputs are left as they are.
+ *   params: [7] complex a0, b, Aq, wq, t, q0, q1.  e_pol_x, e_pol_y, Sx, Sy: device [n]
+ *   c128.  KPM_ERR_INDEX for a column outside [0, n) (that slot is skipped).  Synchronous.
+ */
+int kpm_light_modifier(int64_t count, const double* params, const double* data, const double* dx,
+                       const double* dy, double* data_new, void* stream);
+int kpm_ell_light_update(kpm_ell* h, const double* params, const double* data0, const double* dx,
+                         const double* dy, void* stream);
+int kpm_phonon_modifier(int64_t n, int len_row, const double* params, const double* data,
+                        const int32_t* indices, const double* dx, const double* dy,
+                        const double* e_pol_x, const double* e_pol_y, const double* Sx,
+                        const double* Sy, double* data_new, double* dx_new, double* dy_new,
+                        void* stream);
 
 /* ---- reference-compatible host-pointer entry points ---------------------
  * Same names and argument lists as jclsquant/cuda_cython/cuda/obv.h:21-23,27,30,

@@ -30,6 +30,7 @@ KPM_C128F = 2  # complex128 accuracy in float-float arithmetic (moments only)
 KPM_FLAG_DEVICE_PTRS = 1
 KPM_FLAG_SPLIT_DIAG = 2
 KPM_FLAG_DOUBLING = 4
+KPM_FLAG_COMPLEX = 8
 
 DTYPES = {"c128": KPM_C128, "complex128": KPM_C128, "c64": KPM_C64, "complex64": KPM_C64, "c128f": KPM_C128F}
 
@@ -82,6 +83,9 @@ SIGNATURES = {
     "kpm_honeycomb_ell": (_I, [_I, _I, _I, _D, _P, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
     "kpm_ell_gershgorin_partner": (_I, [_I64, _I, _P, _P, _P, _D, ctypes.POINTER(_D), _P]),
     "kpm_ell_scale_values": (_I, [_I64, _D, _P, _P]),
+    "kpm_light_modifier": (_I, [_I64, _P, _P, _P, _P, _P, _P]),
+    "kpm_ell_light_update": (_I, [_P, _P, _P, _P, _P, _P]),
+    "kpm_phonon_modifier": (_I, [_I64, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
     "kpm_batch_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                    ctypes.POINTER(ctypes.c_float), _P]),
     "kpm_batch_check": (_I, [_P, _P]),

@@ -522,16 +522,11 @@ int kpm_ell_set_values(kpm_ell* h, const double* data, unsigned flags, void* str
                                                                                        h->is_real != 0, h->val64,
                                                                                        h->err_flag);
   KPM_CUDA_TRY(cudaGetLastError());
-  if (h->val32) {  // the complex64 copy is rebuilt on its next use
-    KPM_CUDA_TRY(cudaStreamSynchronize(s));
-    cudaFree(h->val32);
-    h->val32 = nullptr;
-  }
   if (stage.p) {
     KPM_CUDA_TRY(cudaStreamSynchronize(s));
     release(stage);
   }
-  return KPM_OK;
+  return values_changed(h, s);
 }
 
 int kpm_adjoint_forward(kpm_ell* h, int R, int M, int ckpt, const double* v, double* mu, void* stream) {

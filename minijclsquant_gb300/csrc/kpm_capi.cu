@@ -278,6 +278,17 @@ __global__ void hermitian_check_kernel(const void* __restrict__ val, const int32
   }
 }
 
+int values_changed(kpm_ell_s* h, cudaStream_t s) {
+  if (h->val32) {  // the complex64 copy is rebuilt on its next use
+    KPM_CUDA_TRY(cudaStreamSynchronize(s));
+    cudaFree(h->val32);
+    h->val32 = nullptr;
+  }
+  if (h->doubling) return check_hermitian(h, s);  // the next DOS call reads the flag
+  h->herm_stale = 1;
+  return KPM_OK;
+}
+
 int check_hermitian(kpm_ell_s* h, cudaStream_t s) {
   DevBuf flag;
   KPM_TRY(ensure(flag, sizeof(unsigned)));
@@ -297,7 +308,10 @@ int check_hermitian(kpm_ell_s* h, cudaStream_t s) {
   if (rc == KPM_OK) rc = check_cuda(cudaMemcpyAsync(&hf, flag.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
   if (rc == KPM_OK) rc = check_cuda(cudaStreamSynchronize(s));
   release(flag);
-  if (rc == KPM_OK) h->hermitian = hf == 0u ? 1 : 0;
+  if (rc == KPM_OK) {
+    h->hermitian = hf == 0u ? 1 : 0;
+    h->herm_stale = 0;
+  }
   return rc;
 }
 
@@ -634,7 +648,8 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
                    unsigned flags, void* stream) {
   if (!out || !data || !indices || n_rows < 1 || len_row < 1) return KPM_ERR_INVALID_ARG;
   if (n_rows > (int64_t)INT32_MAX) return KPM_ERR_SHAPE;
-  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG | KPM_FLAG_DOUBLING)) return KPM_ERR_INVALID_ARG;
+  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG | KPM_FLAG_DOUBLING | KPM_FLAG_COMPLEX))
+    return KPM_ERR_INVALID_ARG;
   *out = nullptr;
   cudaStream_t s = as_stream(stream);
   kpm_ell_s* h = new kpm_ell_s();
@@ -694,7 +709,7 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
   }
   if (hflags & 1u) return fail(KPM_ERR_INDEX);
   if (hflags & 4u) return fail(KPM_ERR_NONFINITE);
-  h->is_real = (hflags & 2u) ? 0 : 1;
+  h->is_real = ((hflags & 2u) || (flags & KPM_FLAG_COMPLEX)) ? 0 : 1;
   const int64_t slots = (int64_t)len_row * h->n_pad;
   e = cudaMalloc(&h->val64, slots * (h->is_real ? sizeof(double) : sizeof(double2)));
   if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->col), slots * sizeof(int32_t));
@@ -1038,6 +1053,7 @@ int kpm_ell_series_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per
 
 int kpm_ell_props(const kpm_ell* h, int* hermitian, int* doubling) {
   if (!h) return KPM_ERR_INVALID_ARG;
+  if (h->herm_stale) KPM_TRY(check_hermitian(const_cast<kpm_ell*>(h), nullptr));  // a cached property
   if (hermitian) *hermitian = h->hermitian;
   if (doubling) *doubling = use_doubling(h, 4) ? 1 : 0;
   return KPM_OK;
@@ -1046,6 +1062,7 @@ int kpm_ell_props(const kpm_ell* h, int* hermitian, int* doubling) {
 int kpm_ell_set_doubling(kpm_ell* h, int on) {
   if (!h) return KPM_ERR_INVALID_ARG;
   h->doubling = on ? 1 : 0;
+  if (h->doubling && h->herm_stale) KPM_TRY(check_hermitian(h, nullptr));
   return KPM_OK;
 }
 

@@ -1,0 +1,219 @@
+// kpm_driven.cu -- time-dependent operators of driven systems on the device.
+//
+//   kpm_light_modifier : the Peierls substitution of a light pulse, the four forms of
+//       light_modifier_cython (jclsquant/cython_modules/Extra_funs.pyx:236-342):
+//         data_new = a * data * exp(i A0 (cx dx + cy dy) / ch)
+//       with (cx, cy) = (0, sin wt) (linear) or (cos wt, eta sin wt) (circular), and
+//       ch = cosh((t - 2 Tp) / (0.5673 Tp)) for the packed (pulse) forms, 1 otherwise.
+//   kpm_ell_light_update : the same H(t) written straight into an operator's stored
+//       values (the doubled SoA layout of kpm_ell_create), so a time-stepping caller
+//       rewrites H(t) in one pass on the device instead of through host arrays.
+//   kpm_phonon_modifier : hopping_pos_phonons_modifier (Extra_funs.pyx:540-560): bond
+//       vectors displaced by a damped phonon, hoppings scaled by exp(-b (|d| / a0 - 1)).
+//
+// The time-dependent scalars (cos wt, sin wt, the pulse envelope) are evaluated once on
+// the host in complex double arithmetic, as the reference evaluates them per element;
+// per element the kernels do complex multiplies and one complex exponential
+// exp(x + iy) = e^x (cos y + i sin y).  Streaming kernels, HBM-bound, run once per time
+// step (recomputing the phases inside every recursion step would add a sincos per slot
+// per step to an FP64-bound kernel).
+#include <algorithm>
+#include <cmath>
+#include <complex>
+
+#include "kpm_internal.cuh"
+
+using namespace kpm;
+
+namespace {
+
+using cplx = std::complex<double>;
+
+inline cudaStream_t stream_of(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline cplx param(const double* p, int k) { return cplx(p[2 * k], p[2 * k + 1]); }
+inline double2 d2(cplx z) { return make_double2(z.real(), z.imag()); }
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cexp2(double2 z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  const double e = z.x == 0.0 ? 1.0 : exp(z.x);  // a pure phase (real pulse parameters): exp(0) = 1
+  return make_double2(e * c, e * s);
+}
+// cos(x + iy) = cos x cosh y - i sin x sinh y
+__device__ __forceinline__ double2 ccos2(double2 z) {
+  double s, c;
+  sincos(z.x, &s, &c);
+  return make_double2(c * cosh(z.y), -s * sinh(z.y));
+}
+// a / b for complex b
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+int grid_for_count(int64_t count) { return (int)std::max<int64_t>(1, std::min<int64_t>((count + 255) / 256, 65536)); }
+
+// Per-element coefficients of the light modifier: z = kx dx + ky dy.
+void light_coefficients(const double* params, double2* a, double2* kx, double2* ky) {
+  const cplx A = param(params, 0), A0 = param(params, 1), t = param(params, 2), w = param(params, 3),
+             Tp = param(params, 4), eta = param(params, 5);
+  const cplx I(0.0, 1.0);
+  const cplx ch = (Tp != 0.0) ? std::cosh((t - 2.0 * Tp) / (0.5673 * Tp)) : cplx(1.0, 0.0);
+  const cplx sw = std::sin(w * t), cw = std::cos(w * t);
+  if (eta == 0.0) {  // linear forms: the y component only
+    *kx = make_double2(0.0, 0.0);
+    *ky = d2(I * A0 * sw / ch);
+  } else {
+    *kx = d2(I * A0 * cw / ch);
+    *ky = d2(I * A0 * eta * sw / ch);
+  }
+  *a = d2(A);
+}
+
+__global__ void light_kernel(int64_t count, double2 a, double2 kx, double2 ky, const double2* __restrict__ data,
+                             const double2* __restrict__ dx, const double2* __restrict__ dy, double2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 z = cadd(cmul(kx, dx[i]), cmul(ky, dy[i]));
+    out[i] = cmul(cmul(a, data[i]), cexp2(z));
+  }
+}
+
+// H(t) into the doubled SoA values of an operator: slot t = s * n_pad + row.
+__global__ void light_update_kernel(int64_t n, int64_t n_pad, int L, double2 a, double2 kx, double2 ky,
+                                    const double2* __restrict__ data, const double2* __restrict__ dx,
+                                    const double2* __restrict__ dy, double2* __restrict__ val) {
+  const int64_t total = (int64_t)L * n_pad;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int s = (int)(t / n_pad);
+    const int64_t row = t - (int64_t)s * n_pad;
+    double2 v = make_double2(0.0, 0.0);
+    if (row < n) {
+      const int64_t k = row * L + s;
+      const double2 z = cadd(cmul(kx, dx[k]), cmul(ky, dy[k]));
+      v = cmul(cmul(a, data[k]), cexp2(z));
+    }
+    val[t] = make_double2(2.0 * v.x, 2.0 * v.y);
+  }
+}
+
+// p[i] = e_pol[i] cos(wt - q Sx[i]), per site (both the row's and the column's term of
+// every bond are read from here).
+__global__ void phonon_site_kernel(int64_t n, double2 wt, double2 q0, double2 q1, const double2* __restrict__ ex,
+                                   const double2* __restrict__ ey, const double2* __restrict__ sx,
+                                   const double2* __restrict__ sy, double2* __restrict__ px, double2* __restrict__ py) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 ax = make_double2(wt.x, wt.y);
+    const double2 qx = cmul(q0, sx[i]);
+    const double2 qy = cmul(q1, sy[i]);
+    px[i] = cmul(ex[i], ccos2(make_double2(ax.x - qx.x, ax.y - qx.y)));
+    py[i] = cmul(ey[i], ccos2(make_double2(ax.x - qy.x, ax.y - qy.y)));
+  }
+}
+
+__global__ void phonon_kernel(int64_t count, int64_t n, int L, double2 aq_over_ch, double2 a0, double2 b,
+                              const double2* __restrict__ data, const int32_t* __restrict__ idx,
+                              const double2* __restrict__ dx, const double2* __restrict__ dy,
+                              const double2* __restrict__ px, const double2* __restrict__ py,
+                              double2* __restrict__ data_new, double2* __restrict__ dx_new,
+                              double2* __restrict__ dy_new, unsigned* bad) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = i / L;
+    const int64_t col = idx[i];
+    if (row == col) continue;  // diagonal slots are left as they are
+    if (col < 0 || col >= n) {  // a column outside the operator: recorded, slot skipped
+      atomicOr(bad, 1u);
+      continue;
+    }
+    const double2 ddx = cmul(aq_over_ch, make_double2(px[row].x - px[col].x, px[row].y - px[col].y));
+    const double2 ddy = cmul(aq_over_ch, make_double2(py[row].x - py[col].x, py[row].y - py[col].y));
+    const double2 nx = cadd(dx[i], ddx), ny = cadd(dy[i], ddy);
+    // r = sqrt(|dx|^2 + |dy|^2) / a0 - 1;  data_new = data exp(-b r)
+    const double len = sqrt(nx.x * nx.x + nx.y * nx.y + ny.x * ny.x + ny.y * ny.y);
+    double2 r = cdiv(make_double2(len, 0.0), a0);
+    r.x -= 1.0;
+    const double2 z = cmul(make_double2(-b.x, -b.y), r);
+    dx_new[i] = nx;
+    dy_new[i] = ny;
+    data_new[i] = cmul(data[i], cexp2(z));
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpm_light_modifier(int64_t count, const double* params, const double* data, const double* dx, const double* dy,
+                       double* data_new, void* stream) {
+  if (count < 1 || !params || !data || !dx || !dy || !data_new) return KPM_ERR_INVALID_ARG;
+  double2 a, kx, ky;
+  light_coefficients(params, &a, &kx, &ky);
+  cudaStream_t s = stream_of(stream);
+  light_kernel<<<grid_for_count(count), 256, 0, s>>>(count, a, kx, ky, reinterpret_cast<const double2*>(data),
+                                                     reinterpret_cast<const double2*>(dx),
+                                                     reinterpret_cast<const double2*>(dy),
+                                                     reinterpret_cast<double2*>(data_new));
+  return check_cuda(cudaGetLastError());
+}
+
+int kpm_ell_light_update(kpm_ell* h, const double* params, const double* data0, const double* dx, const double* dy,
+                         void* stream) {
+  if (!h || !params || !data0 || !dx || !dy) return KPM_ERR_INVALID_ARG;
+  if (h->is_real) return KPM_ERR_DTYPE;  // H(t) is complex: create the operator with KPM_FLAG_COMPLEX
+  double2 a, kx, ky;
+  light_coefficients(params, &a, &kx, &ky);
+  cudaStream_t s = stream_of(stream);
+  light_update_kernel<<<grid_for_count((int64_t)h->L * h->n_pad), 256, 0, s>>>(
+      h->n, h->n_pad, h->L, a, kx, ky, reinterpret_cast<const double2*>(data0), reinterpret_cast<const double2*>(dx),
+      reinterpret_cast<const double2*>(dy), static_cast<double2*>(h->val64));
+  KPM_TRY(check_cuda(cudaGetLastError()));
+  return values_changed(h, s);
+}
+
+int kpm_phonon_modifier(int64_t n, int len_row, const double* params, const double* data, const int32_t* indices,
+                        const double* dx, const double* dy, const double* e_pol_x, const double* e_pol_y,
+                        const double* Sx, const double* Sy, double* data_new, double* dx_new, double* dy_new,
+                        void* stream) {
+  if (n < 1 || len_row < 1 || !params || !data || !indices || !dx || !dy || !e_pol_x || !e_pol_y || !Sx || !Sy ||
+      !data_new || !dx_new || !dy_new)
+    return KPM_ERR_INVALID_ARG;
+  const cplx a0 = param(params, 0), b = param(params, 1), Aq = param(params, 2), wq = param(params, 3),
+             t = param(params, 4), q0 = param(params, 5), q1 = param(params, 6);
+  if (wq == 0.0 || a0 == 0.0) return KPM_ERR_INVALID_ARG;
+  const cplx Tp = 2.0 * M_PI / wq;
+  const cplx ch = std::cosh((t - 2.0 * Tp) / (0.5673 * Tp));
+  cudaStream_t s = stream_of(stream);
+  DevBuf site;
+  KPM_TRY(ensure(site, (size_t)2 * n * sizeof(double2) + sizeof(double2)));
+  double2* px = static_cast<double2*>(site.p);
+  double2* py = px + n;
+  unsigned* bad = reinterpret_cast<unsigned*>(py + n);
+  unsigned bad_host = 0;
+  KPM_TRY(check_cuda(cudaMemsetAsync(bad, 0, sizeof(unsigned), s)));
+  phonon_site_kernel<<<grid_for_count(n), 256, 0, s>>>(n, d2(wq * t), d2(q0), d2(q1),
+                                                       reinterpret_cast<const double2*>(e_pol_x),
+                                                       reinterpret_cast<const double2*>(e_pol_y),
+                                                       reinterpret_cast<const double2*>(Sx),
+                                                       reinterpret_cast<const double2*>(Sy), px, py);
+  int st = check_cuda(cudaGetLastError());
+  const int64_t count = n * (int64_t)len_row;
+  if (st == KPM_OK) {
+    phonon_kernel<<<grid_for_count(count), 256, 0, s>>>(
+        count, n, len_row, d2(Aq / ch), d2(a0), d2(b), reinterpret_cast<const double2*>(data), indices,
+        reinterpret_cast<const double2*>(dx), reinterpret_cast<const double2*>(dy), px, py,
+        reinterpret_cast<double2*>(data_new), reinterpret_cast<double2*>(dx_new), reinterpret_cast<double2*>(dy_new),
+        bad);
+    st = check_cuda(cudaGetLastError());
+  }
+  if (st == KPM_OK) st = check_cuda(cudaMemcpyAsync(&bad_host, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+  if (st == KPM_OK) st = check_cuda(cudaStreamSynchronize(s));  // the per-site scratch is freed below
+  release(site);
+  if (st == KPM_OK && bad_host) st = KPM_ERR_INDEX;
+  return st;
+}
+
+}  // extern "C"

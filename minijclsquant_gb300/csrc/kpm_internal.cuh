@@ -107,6 +107,7 @@ struct kpm_ell_s {
   int adj_R = 0, adj_M = 0, adj_ckpt = 0;
   // H == H^dagger, checked on the device at creation; doubling allowed for DOS moments
   int hermitian = 0;
+  int herm_stale = 0;  // values changed since the last check (checked when doubling or a query needs it)
   int doubling = 0;  // requested (KPM_FLAG_DOUBLING / kpm_ell_set_doubling)
   // process-unique id of this handle, and the id of an operator whose ELL column arrays
   // were found equal to this one's (kpm_mu_nm fuses V T_m into the H step then)
@@ -179,6 +180,9 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
 bool use_doubling(const kpm_ell_s* h, int M);
 int half_norms(const void* packed, bool f32, int64_t n_pad, int Rg, void* hv, cudaStream_t s);
 int check_hermitian(kpm_ell_s* h, cudaStream_t s);
+// After new values: drop the complex64 copy (rebuilt on its next use); H == H^dagger
+// is checked again now when doubling is on, else on the next query (kpm_capi.cu).
+int values_changed(kpm_ell_s* h, cudaStream_t s);
 int doubling_corr(const void* packed, const void* hv, bool f32, int64_t n_pad, int Rg, const int64_t* seg_begin,
                   int nseg, double* corr, cudaStream_t s);
 int mu1_exact(const kpm_ell_s* h, const void* packed_f32, int Rg, const int64_t* seg_begin, int nseg, double2* out,

@@ -41,9 +41,12 @@ def _as_device_c128(x, n: int | None = None) -> torch.Tensor:
 class DeviceELL:
     """A libkpm operator: SoA ELL on the GPU (values doubled, rows padded)."""
 
-    def __init__(self, data, indices, len_row: int, n_rows: int | None = None, *, doubling: bool = False):
+    def __init__(self, data, indices, len_row: int, n_rows: int | None = None, *, doubling: bool = False,
+                 complex_values: bool = False):
         """doubling=True: DOS moments of a Hermitian operator use the doubling
-        identity (ceil(M/2) - 1 recursion steps instead of M - 2)."""
+        identity (ceil(M/2) - 1 recursion steps instead of M - 2).  complex_values=True
+        stores complex values even when every imaginary part is zero (an operator whose
+        values light_update will make complex)."""
         _require_cuda()
         lib = _capi.lib()
         data_is_dev = isinstance(data, torch.Tensor) and data.is_cuda
@@ -71,6 +74,8 @@ class DeviceELL:
             raise ValueError("data and indices differ in length")
         if doubling:
             flags |= _capi.KPM_FLAG_DOUBLING
+        if complex_values:
+            flags |= _capi.KPM_FLAG_COMPLEX
         handle = ctypes.c_void_p()
         torch.cuda.synchronize()
         st = lib.kpm_ell_create(ctypes.byref(handle), n, len_row, dptr, iptr, flags, _stream_ptr())
@@ -96,6 +101,24 @@ class DeviceELL:
         d = ctypes.c_int()
         _capi.check(_capi.lib().kpm_ell_props(self._h, None, ctypes.byref(d)), "kpm_ell_props")
         return bool(d.value)
+
+    def light_update(self, data0, dx, dy, modifier_id, modifier_params, t, stream=None):
+        """Replace the values by H(t) = H0 o exp(i A0 (...)) of a light pulse, computed on
+        the device from H0 = data0 and its bond vectors (kpm_ell_light_update; the forms of
+        jclsquant/modifiers.py:133-182).  The operator must hold complex values."""
+        from .modifiers import _complex_params, _dev, _light_params
+
+        prm = _light_params(modifier_id, modifier_params, t)
+        if prm is None:
+            return None
+        d, x, y = _dev(data0), _dev(dx), _dev(dy)
+        if d.numel() != self.n * self.len_row:
+            raise ValueError("H0 arrays must hold %d entries" % (self.n * self.len_row))
+        p = _complex_params(prm)
+        st = _capi.lib().kpm_ell_light_update(self._h, p.ctypes.data, d.data_ptr(), x.data_ptr(), y.data_ptr(),
+                                              _stream_ptr(stream))
+        _capi.check(st, "kpm_ell_light_update")
+        return self
 
     def set_doubling(self, on: bool):
         _capi.check(_capi.lib().kpm_ell_set_doubling(self._h, int(bool(on))), "kpm_ell_set_doubling")

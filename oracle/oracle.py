@@ -165,3 +165,34 @@ def adjoint_grad(M, data, indices, len_row, v, c):
     _check(lib().oracle_adjoint_grad(int(M), data.ctypes.data, indices.ctypes.data, int(len_row), v.size,
                                      v.ctypes.data, c.ctypes.data, grad.ctypes.data), "adjoint_grad")
     return grad
+
+
+def light_modifier(a, A0, t, w, Tp, eta, data, dx, dy):
+    """The Peierls substitution of light_modifier_cython (jclsquant/cython_modules/
+    Extra_funs.pyx:319-342, the forms at :236-317), in numpy complex arithmetic."""
+    data, dx, dy = (np.asarray(x, dtype=np.complex128) for x in (data, dx, dy))
+    a, A0, t, w, Tp, eta = (complex(x) for x in (a, A0, t, w, Tp, eta))
+    if eta == 0:
+        arg = 1j * A0 * (np.sin(w * t) * dy)  # linear forms (:257-299)
+    else:
+        arg = 1j * A0 * (np.cos(w * t) * dx + eta * np.sin(w * t) * dy)  # circular forms (:236-255, :301-317)
+    if Tp != 0:
+        arg = arg / np.cosh((t - 2 * Tp) / (0.5673 * Tp))
+    return a * data * np.exp(arg)
+
+
+def phonon_modifier(a0, b, Aq, wq, t, q, data, indices, dx, dy, e_pol_x, e_pol_y, Sx, Sy, len_row):
+    """hopping_pos_phonons_modifier (jclsquant/cython_modules/Extra_funs.pyx:540-560):
+    (data_new, dx_new, dy_new); slots on the diagonal keep their values."""
+    data, dx, dy = (np.asarray(x, dtype=np.complex128) for x in (data, dx, dy))
+    indices = np.asarray(indices)
+    Tp = 2 * np.pi / wq
+    ch = np.cosh((t - 2 * Tp) / (0.5673 * Tp))
+    rows = np.arange(data.size) // int(len_row)
+    m = rows != indices
+    r, c = rows[m], indices[m]
+    dn, dxn, dyn = data.copy(), dx.copy(), dy.copy()
+    dxn[m] = dx[m] + Aq * (e_pol_x[r] * np.cos(wq * t - q[0] * Sx[r]) - e_pol_x[c] * np.cos(wq * t - q[0] * Sx[c])) / ch
+    dyn[m] = dy[m] + Aq * (e_pol_y[r] * np.cos(wq * t - q[1] * Sy[r]) - e_pol_y[c] * np.cos(wq * t - q[1] * Sy[c])) / ch
+    dn[m] = data[m] * np.exp(-b * (np.sqrt(np.abs(dxn[m]) ** 2 + np.abs(dyn[m]) ** 2 + 0j) / a0 - 1))
+    return dn, dxn, dyn

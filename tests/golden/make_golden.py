@@ -173,6 +173,7 @@ def main():
          mu_U=km.moments_U(1.3, 40), gmas=np.stack([km.moments_Gmas(e, 16) for e in E]))
 
     time_evolution_case(ref)
+    modifiers_case(ref)
 
 
 def time_evolution_case(ref):
@@ -201,7 +202,46 @@ def time_evolution_case(ref):
          n=np.int64(n), c=c, M=np.int64(M), len_t=np.int64(len_t), U0=U0, Uc0=Uc0, U=U, Uc=Uc)
 
 
-CASES = {"time_evolution_6x5": time_evolution_case}
+def modifiers_case(ref):
+    """9. time-dependent operators of driven systems: the reference's own light modifier
+    (light_modifier_cython, jclsquant/cython_modules/Extra_funs.pyx:236-342) in its four
+    forms and its phonon modifier (hopping_pos_phonons_modifier, Extra_funs.pyx:540-560),
+    on graphene ELL arrays with bond vectors (jclsquant's ell_matrix from CSR)."""
+    m = ref.modifiers
+    arr = lattice.honeycomb_arrays(6, 5, t=-2.7, W=0.3, seed=7)
+    dx = lattice.to_csr(dict(arr, data=arr["dx"]))
+    dy = lattice.to_csr(dict(arr, data=arr["dy"]))
+    H = ref.ell_matrix.ell_matrix(lattice.to_csr(arr), dx, dy, None)
+    size = len(H.data)
+    out = dict(data=H.data, indices=H.indices, len_row=np.int64(H.len_row), dx=H.dx_vec, dy=H.dy_vec)
+    # (a, A0, t, w, Tp, eta): linear, circular (right), linear packed, circular packed (left), complex A0
+    light = np.array([[1, 2.1, 0.37, 1.9, 0, 0], [1, 2.1, 0.37, 1.9, 0, 1], [1, 1.4, 0.9, 2.3, 0.6, 0],
+                      [1, 1.4, 0.9, 2.3, 0.6, -1], [0.5 + 0.2j, 0.7 + 0.05j, 1.1, 0.8, 0.3, 1]], dtype=np.complex128)
+    light_out = []
+    for a, A0, t, w, Tp, eta in light:
+        new = np.zeros(size, dtype=np.complex128)
+        m.light_modifier_cython(a, A0, t, w, Tp, eta, H.data, H.dx_vec, H.dy_vec, new, size, 2)
+        light_out.append(new)
+    out.update(light_params=light, light_out=np.stack(light_out))
+    # phonons: the 'chiral_+' polarisation of modifier_hoppings_c_r (jclsquant/modifiers.py:417-421)
+    n = int(H.shape[0])
+    a0, b, Aq, wq, t = 0.142 + 0j, 3.37 + 0j, 0.01 + 0j, 2.0 + 0j, 0.8 + 0j
+    q = np.array([4 * np.pi / (3 * np.sqrt(3) * 0.142), 0], dtype=np.complex128)
+    ex = np.ascontiguousarray(np.array([1 / np.sqrt(2), 1 / np.sqrt(2)] * (n // 2), dtype=np.complex128))
+    ey = np.ascontiguousarray(np.array([1j / np.sqrt(2), -1j / np.sqrt(2)] * (n // 2), dtype=np.complex128))
+    rng = np.random.default_rng(11)
+    S = rng.uniform(0, 2.0, (n, 2)).astype(np.complex128)
+    d_new, dx_new, dy_new = H.data.copy(), H.dx_vec.copy(), H.dy_vec.copy()
+    m.hopping_pos_phonons_modifier(H.data, H.indices, H.dx_vec, H.dy_vec, d_new, dx_new, dy_new, a0, b, Aq, ex, ey,
+                                   wq, t, np.ascontiguousarray(S[:, 0]), np.ascontiguousarray(S[:, 1]), q, H.len_row,
+                                   size, 2)
+    out.update(phonon_params=np.array([a0, b, Aq, wq, t, q[0], q[1]]), e_pol_x=ex, e_pol_y=ey,
+               Sx=np.ascontiguousarray(S[:, 0]), Sy=np.ascontiguousarray(S[:, 1]), phonon_data=d_new,
+               phonon_dx=dx_new, phonon_dy=dy_new)
+    save("modifiers_6x5", **out)
+
+
+CASES = {"time_evolution_6x5": time_evolution_case, "modifiers_6x5": modifiers_case}
 
 
 if __name__ == "__main__":

@@ -156,3 +156,17 @@ def test_oracle_known_answers():
     ref = np.array([0.5 * np.vdot(v, np.roll(v, -m) + np.roll(v, m)) for m in range(M)])
     assert oracle.moment_tolerance_ok(mu, ref, 1e-10)[0]
     assert abs(mu[0] - n) <= 1e-12 * n
+
+
+def test_oracle_modifiers_match_reference():
+    """The light and phonon modifiers against the reference's own Cython outputs."""
+    z = golden("modifiers_6x5")
+    for prm, want in zip(z["light_params"], z["light_out"]):
+        got = oracle.light_modifier(*prm, z["data"], z["dx"], z["dy"])
+        assert np.max(np.abs(got - want)) <= 1e-14 * np.max(np.abs(want)), prm
+    a0, b, Aq, wq, t, q0, q1 = z["phonon_params"]
+    dn, dxn, dyn = oracle.phonon_modifier(a0, b, Aq, wq, t, np.array([q0, q1]), z["data"], z["indices"], z["dx"],
+                                          z["dy"], z["e_pol_x"], z["e_pol_y"], z["Sx"], z["Sy"], int(z["len_row"]))
+    assert np.max(np.abs(dn - z["phonon_data"])) <= 1e-14 * np.max(np.abs(z["phonon_data"]))
+    assert np.max(np.abs(dxn - z["phonon_dx"])) <= 1e-14 * np.max(np.abs(z["phonon_dx"]))
+    assert np.max(np.abs(dyn - z["phonon_dy"])) <= 1e-14 * np.max(np.abs(z["phonon_dy"]))

@@ -42,7 +42,7 @@ extern "C" {
 #define KPM_ERR_CUDA 5          /* a CUDA runtime call or launch failed       */
 #define KPM_ERR_TIMEOUT 6       /* a bounded device-side wait gave up         */
 #define KPM_ERR_INDEX 7         /* an ELL column index is outside [0, n)      */
-#define KPM_ERR_UNSUPPORTED 8   /* valid request this build does not serve    */
+#define KPM_ERR_UNSUPPORTED 8   /* valid request the library does not serve   */
 #define KPM_ERR_NONFINITE 9     /* a moment came out NaN or Inf               */
 #define KPM_ERR_TOO_LARGE 10    /* beyond the fixed scratch of kpm_cheb_moments_noalloc */
 

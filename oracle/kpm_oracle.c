@@ -1,9 +1,9 @@
 /*
  * kpm_oracle.c -- TEST INFRASTRUCTURE ONLY.
  *
- * A plain-C (C99 + OpenMP) restatement of jclsquant's CPU hot path, used as
- * the checker for the CUDA kernels and as the CPU baseline ("port") in the
- * benchmark.  Nothing in the product library links or calls this file.
+ * A plain-C (C99 + OpenMP) restatement of jclsquant's CPU hot path: the
+ * oracle the tests hold the CUDA kernels to, and the CPU baseline ("port") in
+ * the benchmark.  Nothing in the product library links or calls this file.
  *
  * Every function follows one reference routine; the citation is given on
  * each.  The loop structure (per-row accumulation order inside the SpMV,

@@ -1,7 +1,7 @@
 """numpy-facing wrapper of the C oracle -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py``
-use this module, as the checker (and the CPU baseline "port"); the product
+use this module, as the oracle (and the CPU baseline "port"); the product
 library never imports it.  Each function follows the reference routine named
 in its docstring (the C file gives file:line for each).
 """

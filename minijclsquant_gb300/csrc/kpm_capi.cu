@@ -3,6 +3,7 @@
 // reference-compatible host-pointer entry points.
 #include <algorithm>
 #include <atomic>
+#include <mutex>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -25,16 +26,24 @@ thread_local int g_last_status = KPM_OK;
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 // ---- ELL ingest -------------------------------------------------------------
+// Flags (bad column, complex value, non-finite value) and a fingerprint of the column
+// structure: the wrapping sum of (column - row) * (2 slot + 1), order-independent, so
+// operators of one shape and sparsity share their tuned step kernels.
 __global__ void ell_validate_kernel(const double2* __restrict__ data, const int32_t* __restrict__ idx, int64_t count,
-                                    int64_t n, unsigned* flags) {
+                                    int64_t n, int L, unsigned* flags, unsigned long long* fingerprint) {
   unsigned f = 0;
+  unsigned long long fp = 0;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
     const int32_t c = idx[t];
     if (c < 0 || (int64_t)c >= n) f |= 1u;
     if (data[t].y != 0.0) f |= 2u;
     if (!isfinite(data[t].x) || !isfinite(data[t].y)) f |= 4u;
+    const int64_t row = t / L;
+    fp += (unsigned long long)((int64_t)c - row) * (unsigned long long)(2 * (t - row * L) + 1);
   }
   if (f) atomicOr(flags, f);
+  for (int o = 16; o > 0; o >>= 1) fp += __shfl_xor_sync(0xffffffffu, fp, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(fingerprint, fp);
 }
 
 // AoS [row][slot] -> SoA [slot][n_pad], values doubled (exact).
@@ -113,6 +122,23 @@ int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepPar
 // sets: 1 one moment set, 2 two sets, 3 doubled moments, 4 a series step (no
 // moments; series += c_m T_{m+1}).  Timing clears ws.ta, ws.tb and ws.vl (and ws.vr
 // for sets 2 and 3): callers tune before they fill those.
+// Step choices shared by the handles of one process: operators of equal shape, value
+// type and column structure (kpm_ell_s::structure) on one device time the same.
+struct TunedShape {
+  int device;
+  int64_t n_pad;
+  int L, is_real, key;
+  uint64_t structure;
+  StepConfig cfg;
+};
+static std::mutex g_tuned_mu;
+static std::vector<TunedShape> g_tuned;
+
+static bool same_shape(const TunedShape& t, const kpm_ell_s* h, int key) {
+  return t.device == h->device && t.n_pad == h->n_pad && t.L == h->L && t.is_real == h->is_real && t.key == key &&
+         t.structure == h->structure;
+}
+
 int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out) {
   const int key = (f32 ? 1000 : 0) + Rg * 10 + sets;
   for (auto& kv : h->tuned)
@@ -123,6 +149,15 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
   std::vector<StepConfig> cands;
   const char* force = getenv("KPM_STEP_KERNEL");
   const std::string f = force ? force : "";
+  if (f.empty()) {  // an operator of this shape was tuned before in this process
+    std::lock_guard<std::mutex> lock(g_tuned_mu);
+    for (auto& t : g_tuned)
+      if (same_shape(t, h, key)) {
+        h->tuned.emplace_back(key, t.cfg);
+        *out = t.cfg;
+        return KPM_OK;
+      }
+  }
   if (f.empty() || f == "simple") {
     StepConfig c;
     c.kind = 0;
@@ -203,6 +238,10 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
   for (auto& c : cands)
     if (c.us < best.us) best = c;
   h->tuned.emplace_back(key, best);
+  if (f.empty()) {
+    std::lock_guard<std::mutex> lock(g_tuned_mu);
+    g_tuned.push_back(TunedShape{h->device, h->n_pad, h->L, h->is_real, key, h->structure, best});
+  }
   *out = best;
   return KPM_OK;
 }
@@ -692,21 +731,25 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
     d_data = static_cast<const double2*>(stage_data.p);
     d_idx = static_cast<const int32_t*>(stage_idx.p);
   }
-  if ((st = ensure(flag_buf, sizeof(unsigned))) != KPM_OK) return fail(st);
-  e = cudaMemsetAsync(flag_buf.p, 0, sizeof(unsigned), s);
+  if ((st = ensure(flag_buf, 2 * sizeof(unsigned long long))) != KPM_OK) return fail(st);
+  e = cudaMemsetAsync(flag_buf.p, 0, 2 * sizeof(unsigned long long), s);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
     return fail(KPM_ERR_CUDA);
   }
-  ell_validate_kernel<<<grid_1d(count), 256, 0, s>>>(d_data, d_idx, count, n_rows, static_cast<unsigned*>(flag_buf.p));
-  unsigned hflags = 0;
+  ell_validate_kernel<<<grid_1d(count), 256, 0, s>>>(d_data, d_idx, count, n_rows, len_row,
+                                                     static_cast<unsigned*>(flag_buf.p),
+                                                     static_cast<unsigned long long*>(flag_buf.p) + 1);
+  unsigned long long hbuf[2] = {0, 0};
   e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&hflags, flag_buf.p, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hbuf, flag_buf.p, sizeof(hbuf), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
     return fail(KPM_ERR_CUDA);
   }
+  const unsigned hflags = static_cast<unsigned>(hbuf[0] & 0xffffffffull);
+  h->structure = hbuf[1];
   if (hflags & 1u) return fail(KPM_ERR_INDEX);
   if (hflags & 4u) return fail(KPM_ERR_NONFINITE);
   h->is_real = ((hflags & 2u) || (flags & KPM_FLAG_COMPLEX)) ? 0 : 1;
@@ -732,7 +775,11 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
   release(stage_idx);
   release(flag_buf);
   h->doubling = (flags & KPM_FLAG_DOUBLING) ? 1 : 0;
-  if ((st = check_hermitian(h, s)) != KPM_OK) return fail(st);
+  if (h->doubling) {
+    if ((st = check_hermitian(h, s)) != KPM_OK) return fail(st);
+  } else {
+    h->herm_stale = 1;  // checked when doubling is switched on or the property is read
+  }
   *out = h;
   return KPM_OK;
 }

@@ -113,6 +113,8 @@ struct kpm_ell_s {
   // were found equal to this one's (kpm_mu_nm fuses V T_m into the H step then)
   uint64_t id = 0;
   uint64_t same_cols_id = 0;
+  // fingerprint of the column structure (sum of (column - row) * (2 slot + 1))
+  uint64_t structure = 0;
 };
 
 namespace kpm {

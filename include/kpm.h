@@ -95,7 +95,9 @@ int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M);
 int kpm_ell_check(kpm_ell* h, void* stream);
 /* The recursion-step kernel chosen for (dtype, R): kind 0 = grid-stride,
  * 1 = bulk-copy staged, 2 = bulk-copy staged with a producer warp; rows per
- * thread per tile; CTAs; measured us per step. */
+ * thread per tile; CTAs; measured us per step.  A choice is timed once per
+ * operator shape and column structure in a process and shared by later handles
+ * (KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2 forces one and bypasses that). */
 int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                         float* step_us);
 /* The same for the series step (kpm_cheb_series, kpm_time_evolve, kpm_time_sigma):
@@ -103,8 +105,9 @@ int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_t
 int kpm_ell_series_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                           float* step_us);
 /* Doubling (opt-in: KPM_FLAG_DOUBLING at creation or kpm_ell_set_doubling).
- * kpm_ell_create checks on the device whether H == H^dagger exactly (entry by
- * entry, duplicate slots summed).  For such an operator with doubling on, moment
+ * Whether H == H^dagger exactly (entry by entry, duplicate slots summed) is checked on
+ * the device: at creation when KPM_FLAG_DOUBLING is given, else when doubling is
+ * switched on or kpm_ell_props is first called (and again after new values).  For such an operator with doubling on, moment
  * calls with v_l == NULL and mu_rr == NULL (DOS moments, M >= 4) use
  *   mu_{2k} = 2 sum_i (|t_k,i|^2 - |v_i|^2/2),  mu_{2k+1} = 2 <t_{k+1}|t_k> - mu_1,
  * t_k = T_k(H) v: ceil(M/2) - 1 recursion steps instead of M - 2.  complex128

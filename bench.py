@@ -422,12 +422,27 @@ def run_time_sigma(a, hbm_peak, world):
     torch.cuda.synchronize()
     ms = max_over_ranks(e0.elapsed_time(e1), world) / a.steps
     site_steps = float(n) * ((M - 1) + 2 * (M2 - 1) * (len_t - 1))
+    # the same call in float-float complex128 (KPM_C128F): commutator series, series and
+    # correlator on the FP32 pipe
+    sig_f = device.time_sigma(Hk, V1, V2, cu, M2, cfd, M, 2, v, dtype="c128f")
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(a.steps):
+        sig_f = device.time_sigma(Hk, V1, V2, cu, M2, cfd, M, len_t, v, dtype="c128f")
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_f = max_over_ranks(f0.elapsed_time(f1), world) / a.steps
     blk = {"value": site_steps * world / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
            "config": {"lattice": "honeycomb %dx%d cells (%d sites), W=%g" % (a.sigma_cells, a.sigma_cells, n, a.W),
                       "M": M, "M2": M2, "len_t": len_t, "dt_kpm": dt_kpm, "vectors": 1},
            "gpu_launches": (M + 1) + (len_t - 1) * (M2 + 2) + 2 * len_t,
            "sigma_0": [float(np.real(sig.cpu().numpy()[0])), float(np.imag(sig.cpu().numpy()[0]))],
-           "note": "U and U_c advance as one set of two vectors through the autotuned series step"}
+           "note": "U and U_c advance as one set of two vectors through the autotuned series step",
+           "c128f": {"value": site_steps * world / (ms_f * 1e-3), "ms_per_step": ms_f,
+                     "max_abs_diff_vs_c128_over_max": float(torch.max(torch.abs(sig_f - sig)) / torch.max(torch.abs(sig))),
+                     "note": "dtype KPM_C128F: float pairs (~48 bits) on the FP32 pipe; opt-in"}}
     if not a.no_cpu and world == 1:
         from oracle import oracle
 

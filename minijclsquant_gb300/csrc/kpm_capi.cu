@@ -660,6 +660,28 @@ int series_packed(kpm_ell_s* h, bool f32, int Rg, int M, const double2* coef, co
 
 int check_dtype(int dtype) { return (dtype == KPM_C128 || dtype == KPM_C64) ? KPM_OK : KPM_ERR_DTYPE; }
 
+// U (slots 0..Rg-1) and U_c (slots Rg..2Rg-1) of one packed set [n_pad][2 Rg], joined from
+// or split into two sets [n_pad][Rg].
+__global__ void join_split_kernel(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, int join) {
+  const int64_t total = n_pad * 2 * Rg;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = t / (2 * Rg);
+    const int r = (int)(t - i * 2 * Rg);
+    double2* half = r < Rg ? a : b;
+    const int64_t k = i * Rg + (r < Rg ? r : r - Rg);
+    if (join) both[t] = half[k];
+    else half[k] = both[t];
+  }
+}
+
+int join_split(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, bool join, cudaStream_t s) {
+  const int64_t total = n_pad * 2 * Rg;
+  const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
+  join_split_kernel<<<grid, 256, 0, s>>>(a, b, both, n_pad, Rg, join ? 1 : 0);
+  KPM_CUDA_TRY(cudaGetLastError());
+  return KPM_OK;
+}
+
 }  // namespace kpm
 
 extern "C" {
@@ -966,8 +988,16 @@ int kpm_time_evolve(kpm_ell* h, int dtype, int R, int M, const double* c, int st
 int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M, const double* c, const double* v,
                                double* out, void* stream) {
   if (!h || !v_op || !c || !v || !out || R < 1 || M < 2) return KPM_ERR_INVALID_ARG;
-  KPM_TRY(check_dtype(dtype));
   if (v_op->n != h->n) return KPM_ERR_SHAPE;
+  if (dtype == KPM_C128F) {
+    for (int r0 = 0; r0 < R;) {
+      const int Rg = pow2_group(R - r0);
+      KPM_TRY(comm_series_group_ff(h, v_op, R, r0, Rg, M, c, v, out, as_stream(stream)));
+      r0 += Rg;
+    }
+    return KPM_OK;
+  }
+  KPM_TRY(check_dtype(dtype));
   if (dtype != KPM_C128) return KPM_ERR_UNSUPPORTED;
   cudaStream_t s = as_stream(stream);
   for (int r0 = 0; r0 < R;) {
@@ -984,36 +1014,22 @@ int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int 
   return KPM_OK;
 }
 
-// U (slots 0..Rg-1) and U_c (slots Rg..2Rg-1) of one packed set [n_pad][2 Rg], joined from
-// or split into two sets [n_pad][Rg].
-__global__ void join_split_kernel(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, int join) {
-  const int64_t total = n_pad * 2 * Rg;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = t / (2 * Rg);
-    const int r = (int)(t - i * 2 * Rg);
-    double2* half = r < Rg ? a : b;
-    const int64_t k = i * Rg + (r < Rg ? r : r - Rg);
-    if (join) both[t] = half[k];
-    else half[k] = both[t];
-  }
-}
-
-int join_split(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, bool join, cudaStream_t s) {
-  const int64_t total = n_pad * 2 * Rg;
-  const int grid = (int)std::min<int64_t>((total + 255) / 256, 4096);
-  join_split_kernel<<<grid, 256, 0, s>>>(a, b, both, n_pad, Rg, join ? 1 : 0);
-  KPM_CUDA_TRY(cudaGetLastError());
-  return KPM_OK;
-}
-
 int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u, int M2,
                    const double* c_fd, int M, int len_t, const double* v, double* sigma, void* stream) {
   if (!h || !v1 || !v2 || !c_u || !c_fd || !v || !sigma || R < 1 || M < 2 || M2 < 2 || len_t < 1)
     return KPM_ERR_INVALID_ARG;
-  KPM_TRY(check_dtype(dtype));
-  if (dtype != KPM_C128) return KPM_ERR_UNSUPPORTED;
   if (v1->n != h->n || v2->n != h->n) return KPM_ERR_SHAPE;
   cudaStream_t s = as_stream(stream);
+  if (dtype == KPM_C128F) {
+    for (int r0 = 0; r0 < R;) {
+      const int Rg = std::min(pow2_group(R - r0), kMaxGroupR / 2);
+      KPM_TRY(time_sigma_group_ff(h, v1, v2, R, r0, Rg, c_u, M2, c_fd, M, len_t, v, sigma, s));
+      r0 += Rg;
+    }
+    return KPM_OK;
+  }
+  KPM_TRY(check_dtype(dtype));
+  if (dtype != KPM_C128) return KPM_ERR_UNSUPPORTED;
   for (int r0 = 0; r0 < R;) {
     // U and U_c advance together as one set of 2 Rg vectors: one pass over H per order
     const int Rg = std::min(pow2_group(R - r0), kMaxGroupR / 2);

@@ -504,7 +504,260 @@ int ff_series_packed(kpm_ell_s* h, int Rg, int M, const StepConfig& cfg, const d
   return KPM_OK;
 }
 
+// ---- commutator series and time-domain Kubo in float-float arithmetic ----------------
+struct CommFFParams {
+  const void* val_h;
+  const int32_t* col_h;
+  const void* val_v;
+  const int32_t* col_v;
+  int64_t ld;
+  int Lh, Lv;
+  int64_t n_pad;
+  const float4* tcur;  // T_{m-1}            [n_pad][R]
+  float4* tout;        // T_{m-2} -> T_m
+  const float4* ccur;  // C_{m-1}
+  float4* cout;        // C_{m-2} -> C_m (FIRST: C_1)
+  float4* acc;         // series accumulator
+  const double2* coef;
+  int m;
+};
+
+// One order of rec_com_A_vec (jclsquant/recurrence_functions.py:146-196):
+//   C_m = 2H C_{m-1} - C_{m-2} + 2V T_{m-1},  T_m = 2H T_{m-1} - T_{m-2},  acc += c_m C_m,
+// at m = 1: T_1 = H v, C_1 = V v, acc = c_1 C_1 -- the step of kpm_comm.cu in float pairs
+// (values: the exact float pairs of 2H and 2V).
+template <bool RH, bool RV, int R, bool FIRST>
+__global__ void __launch_bounds__(kBlock) ff_comm_kernel(const CommFFParams p) {
+  using MVH = typename FFVal<RH>::type;
+  using MVV = typename FFVal<RV>::type;
+  constexpr int RPB = kBlock / R;
+  const int sub = threadIdx.x % R, rl = threadIdx.x / R;
+  const MVH* __restrict__ vh = static_cast<const MVH*>(p.val_h);
+  const MVV* __restrict__ vv = static_cast<const MVV*>(p.val_v);
+  const float4 cm = ff_coef(p.coef, p.m);
+  for (int64_t row = (int64_t)blockIdx.x * RPB + rl; row < p.n_pad; row += (int64_t)gridDim.x * RPB) {
+    const int64_t vi = row * R + sub;
+    FF t{0.f, 0.f, 0.f, 0.f}, c{0.f, 0.f, 0.f, 0.f};
+    if (!FIRST) {
+      const FF to = ff_of(p.tout[vi]), co = ff_of(p.cout[vi]);
+      t = FF{-to.rh, -to.ih, -to.rl, -to.il};
+      c = FF{-co.rh, -co.ih, -co.rl, -co.il};
+    }
+    for (int s = 0; s < p.Lh; ++s) {
+      const int32_t j = __ldcs(p.col_h + (int64_t)s * p.ld + row);
+      const MVH hv = __ldcs(vh + (int64_t)s * p.ld + row);
+      ff_mac(t, hv, ff_of(__ldg(p.tcur + (int64_t)j * R + sub)));
+      if (!FIRST) ff_mac(c, hv, ff_of(__ldg(p.ccur + (int64_t)j * R + sub)));
+    }
+    for (int s = 0; s < p.Lv; ++s) {
+      const int32_t j = __ldcs(p.col_v + (int64_t)s * p.ld + row);
+      const MVV w = __ldcs(vv + (int64_t)s * p.ld + row);
+      ff_mac(c, w, ff_of(__ldg(p.tcur + (int64_t)j * R + sub)));
+    }
+    ff_norm(t.rh, t.rl);
+    ff_norm(t.ih, t.il);
+    ff_norm(c.rh, c.rl);
+    ff_norm(c.ih, c.il);
+    if (FIRST) {  // the values are doubled: halve (exact)
+      t = FF{0.5f * t.rh, 0.5f * t.ih, 0.5f * t.rl, 0.5f * t.il};
+      c = FF{0.5f * c.rh, 0.5f * c.ih, 0.5f * c.rl, 0.5f * c.il};
+    }
+    p.tout[vi] = ff_raw(t);
+    p.cout[vi] = ff_raw(c);
+    FF a{0.f, 0.f, 0.f, 0.f};
+    if (!FIRST) a = ff_of(p.acc[vi]);
+    ff_series_add(a, cm, c);
+    p.acc[vi] = ff_raw(a);
+  }
+}
+
+template <bool RH, bool RV, int R>
+int ff_comm_r(bool first, const CommFFParams& p, int grid, cudaStream_t s) {
+  if (first)
+    ff_comm_kernel<RH, RV, R, true><<<grid, kBlock, 0, s>>>(p);
+  else
+    ff_comm_kernel<RH, RV, R, false><<<grid, kBlock, 0, s>>>(p);
+  return check_cuda(cudaGetLastError());
+}
+
+template <bool RH, bool RV>
+int ff_comm_hv(int R, bool first, const CommFFParams& p, int grid, cudaStream_t s) {
+  switch (R) {
+    case 1: return ff_comm_r<RH, RV, 1>(first, p, grid, s);
+    case 2: return ff_comm_r<RH, RV, 2>(first, p, grid, s);
+    case 4: return ff_comm_r<RH, RV, 4>(first, p, grid, s);
+    case 8: return ff_comm_r<RH, RV, 8>(first, p, grid, s);
+    default: return KPM_ERR_UNSUPPORTED;
+  }
+}
+
+int ff_comm_launch(bool rh, bool rv, int R, bool first, const CommFFParams& p, int grid, cudaStream_t s) {
+  if (rh && rv) return ff_comm_hv<true, true>(R, first, p, grid, s);
+  if (rh) return ff_comm_hv<true, false>(R, first, p, grid, s);
+  if (rv) return ff_comm_hv<false, true>(R, first, p, grid, s);
+  return ff_comm_hv<false, false>(R, first, p, grid, s);
+}
+
+// Commutator series of one packed float-pair set x into `result` (float pairs); the
+// recursion uses ws.ta / ws.tc (T) and ws.td / ws.acc2 (C) of h.
+int ff_comm_series_packed(kpm_ell_s* h, kpm_ell_s* v, int Rg, int M, const double2* coef, const float4* x,
+                          float4* result, cudaStream_t s) {
+  const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tc, vb));
+  KPM_TRY(ensure(ws.td, vb));
+  KPM_TRY(ensure(ws.acc2, vb));
+  float4* t_a = static_cast<float4*>(ws.ta.p);
+  float4* t_b = static_cast<float4*>(ws.tc.p);
+  float4* c_a = static_cast<float4*>(ws.td.p);
+  float4* c_b = static_cast<float4*>(ws.acc2.p);
+  KPM_CUDA_TRY(cudaMemcpyAsync(t_a, x, vb, cudaMemcpyDeviceToDevice, s));
+  KPM_CUDA_TRY(cudaMemsetAsync(c_a, 0, vb, s));  // C_0 = [V, T_0] = 0: read as C_{m-2} at m = 2
+  const int grid = grid_for(h, Rg, 1);
+  CommFFParams p;
+  p.val_h = h->val32;
+  p.col_h = h->col;
+  p.val_v = v->val32;
+  p.col_v = v->col;
+  p.ld = h->n_pad;
+  p.Lh = h->L;
+  p.Lv = v->L;
+  p.n_pad = h->n_pad;
+  p.coef = coef;
+  p.acc = result;
+  p.tcur = t_a;  // m = 1: T_1 = H v, C_1 = V v, acc = c_1 C_1
+  p.tout = t_b;
+  p.ccur = nullptr;
+  p.cout = c_b;
+  p.m = 1;
+  KPM_TRY(ff_comm_launch(h->is_real != 0, v->is_real != 0, Rg, true, p, grid, s));
+  for (int m = 2; m < M; ++m) {  // T: t_b -> t_a (in place over T_{m-2}); C: c_b -> c_a
+    p.tcur = t_b;
+    p.tout = t_a;
+    p.ccur = c_b;
+    p.cout = c_a;
+    p.m = m;
+    KPM_TRY(ff_comm_launch(h->is_real != 0, v->is_real != 0, Rg, false, p, grid, s));
+    std::swap(t_a, t_b);
+    std::swap(c_a, c_b);
+  }
+  return KPM_OK;
+}
+
+// sigma partials: per CTA sum of conj(U_c) (V1 U) over its rows, in float pairs then FP64
+// ([grid][R] double2); V1 values are the doubled float pairs (halved at the end, exact).
+template <bool RV, int R>
+__global__ void __launch_bounds__(kBlock) ff_corr_kernel(const void* val, const int32_t* __restrict__ col, int64_t ld,
+                                                         int L, int64_t n_pad, const float4* __restrict__ u,
+                                                         const float4* __restrict__ uc, double2* part) {
+  using MV = typename FFVal<RV>::type;
+  constexpr int RPB = kBlock / R;
+  __shared__ double2 red[(kBlock / 32) * R];
+  const int sub = threadIdx.x % R, rl = threadIdx.x / R;
+  const MV* __restrict__ vv = static_cast<const MV*>(val);
+  double mr[1] = {0.0}, mi[1] = {0.0};
+  FFMom mom{0.f, 0.f, 0.f, 0.f};
+  int pending = 0;
+  for (int64_t row = (int64_t)blockIdx.x * RPB + rl; row < n_pad; row += (int64_t)gridDim.x * RPB) {
+    FF y{0.f, 0.f, 0.f, 0.f};
+    for (int s = 0; s < L; ++s) {
+      const int32_t j = __ldcs(col + (int64_t)s * ld + row);
+      ff_mac(y, __ldcs(vv + (int64_t)s * ld + row), ff_of(__ldg(u + (int64_t)j * R + sub)));
+    }
+    ff_norm(y.rh, y.rl);
+    ff_norm(y.ih, y.il);
+    y = FF{0.5f * y.rh, 0.5f * y.ih, 0.5f * y.rl, 0.5f * y.il};
+    ff_cdot(mom, ff_of(__ldg(uc + row * R + sub)), y);
+    if (++pending == kFfFlush) {
+      pending = 0;
+      ff_fold(mr[0], mi[0], mom);
+    }
+  }
+  ff_fold(mr[0], mi[0], mom);
+  block_reduce_store<R, 1>(mr, mi, part + (int64_t)blockIdx.x * R, red);
+}
+
+int ff_corr_launch(bool rv, int R, const kpm_ell_s* v1, const float4* u, const float4* uc, double2* part, int grid,
+                   cudaStream_t s) {
+#define KPM_FFC(RR)                                                                                             \
+  if (rv)                                                                                                       \
+    ff_corr_kernel<true, RR><<<grid, kBlock, 0, s>>>(v1->val32, v1->col, v1->n_pad, v1->L, v1->n_pad, u, uc,    \
+                                                     part);                                                      \
+  else                                                                                                          \
+    ff_corr_kernel<false, RR><<<grid, kBlock, 0, s>>>(v1->val32, v1->col, v1->n_pad, v1->L, v1->n_pad, u, uc,   \
+                                                      part);                                                     \
+  return check_cuda(cudaGetLastError())
+  switch (R) {
+    case 1: KPM_FFC(1);
+    case 2: KPM_FFC(2);
+    case 4: KPM_FFC(4);
+    case 8: KPM_FFC(8);
+    default: return KPM_ERR_UNSUPPORTED;
+  }
+#undef KPM_FFC
+}
+
 }  // namespace
+
+// Commutator series (rec_com_A_vec) of vectors r0 .. r0 + Rg in float-float arithmetic.
+int comm_series_group_ff(kpm_ell_s* h, kpm_ell_s* v, int R, int r0, int Rg, int M, const double* c, const double* x,
+                         double* out, cudaStream_t s) {
+  KPM_TRY(ensure_f32_values(h, s));
+  KPM_TRY(ensure_f32_values(v, s));
+  const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.vl, vb));
+  KPM_TRY(ensure(ws.acc, vb));
+  KPM_TRY(ff_pack(x, h->n, h->n_pad, R, r0, Rg, ws.vl.p, s));
+  KPM_TRY(ff_comm_series_packed(h, v, Rg, M, reinterpret_cast<const double2*>(c), static_cast<const float4*>(ws.vl.p),
+                                static_cast<float4*>(ws.acc.p), s));
+  const int64_t total = h->n * Rg;
+  const int g = (int)std::min<int64_t>((total + 255) / 256, 65536);
+  ff_unpack_kernel<<<g, 256, 0, s>>>(static_cast<const float4*>(ws.acc.p), h->n, Rg, r0,
+                                     reinterpret_cast<double2*>(out));
+  return check_cuda(cudaGetLastError());
+}
+
+// Time-domain Kubo correlator of vectors r0 .. r0 + Rg (Rg <= 4) in float-float arithmetic:
+// U_c(t_0) by the commutator series, U and U_c advanced as one set of 2 Rg vectors by the
+// series with c_u, sigma[r][j] = <U_c(t_j)|V1 U(t_j)> reduced in FP64.
+int time_sigma_group_ff(kpm_ell_s* h, kpm_ell_s* v1, kpm_ell_s* v2, int R, int r0, int Rg, const double* c_u, int M2,
+                        const double* c_fd, int M, int len_t, const double* v, double* sigma, cudaStream_t s) {
+  KPM_TRY(ensure_f32_values(h, s));
+  KPM_TRY(ensure_f32_values(v1, s));
+  KPM_TRY(ensure_f32_values(v2, s));
+  const size_t vb = (size_t)h->n_pad * Rg * sizeof(float4);
+  Workspace& ws = h->ws;
+  StepConfig cfg;
+  if (M2 > 2) KPM_TRY(ff_config(h, 2 * Rg, true, s, &cfg));  // before the buffers its timing clears are filled
+  KPM_TRY(ensure(ws.vr, vb));        // U
+  KPM_TRY(ensure(ws.acc, vb));       // U_c
+  KPM_TRY(ensure(ws.td, 2 * vb));    // joined state (also commutator scratch)
+  KPM_TRY(ensure(ws.acc2, 2 * vb));  // the next joined state (likewise)
+  const int grid = grid_for(v1, Rg, 1);
+  KPM_TRY(ensure(ws.part, (size_t)grid * Rg * sizeof(double2)));
+  KPM_TRY(ff_pack(v, h->n, h->n_pad, R, r0, Rg, ws.vr.p, s));
+  KPM_TRY(ff_comm_series_packed(h, v2, Rg, M, reinterpret_cast<const double2*>(c_fd),
+                                static_cast<const float4*>(ws.vr.p), static_cast<float4*>(ws.acc.p), s));
+  double* outs[2] = {sigma, sigma};
+  double2* U = static_cast<double2*>(ws.vr.p);  // 16-byte entries: float pairs moved as double2
+  double2* Uc = static_cast<double2*>(ws.acc.p);
+  void* cur = ws.td.p;
+  void* nxt = ws.acc2.p;
+  for (int j = 0; j < len_t; ++j) {
+    if (j > 0) {
+      if (j == 1) KPM_TRY(join_split(U, Uc, static_cast<double2*>(cur), h->n_pad, Rg, true, s));
+      KPM_TRY(ff_series_packed(h, 2 * Rg, M2, cfg, reinterpret_cast<const double2*>(c_u), cur, nxt, s));
+      std::swap(cur, nxt);
+      KPM_TRY(join_split(U, Uc, static_cast<double2*>(cur), h->n_pad, Rg, false, s));
+    }
+    KPM_TRY(ff_corr_launch(v1->is_real != 0, Rg, v1, reinterpret_cast<const float4*>(U),
+                           reinterpret_cast<const float4*>(Uc), static_cast<double2*>(ws.part.p), grid, s));
+    KPM_TRY(reduce_partials(static_cast<double2*>(ws.part.p), 1, 1, grid, Rg, outs, R, r0, len_t, j, s));
+  }
+  return KPM_OK;
+}
 
 // out[r] = P^steps v[r], P = sum_{m<M} c_m T_m(H), for vectors r0 .. r0 + Rg in float-float
 // arithmetic (steps = 1: the series of rec_A_vec).  The state ping-pongs between ws.tc and

@@ -200,6 +200,12 @@ int moments_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* v
 // launch == false only checks that the form fits (KPM_ERR_UNSUPPORTED otherwise).
 int kubo_step(bool real_h, int R, const StepParams& p, const void* vval, void* bout, int sm_count, cudaStream_t s,
               bool launch);
+// KPM_C128F: the commutator series and the time-domain Kubo correlator of one vector
+// group (kpm_ff.cu); time_sigma_group_ff needs Rg <= 4.
+int comm_series_group_ff(kpm_ell_s* h, kpm_ell_s* v, int R, int r0, int Rg, int M, const double* c, const double* x,
+                         double* out, cudaStream_t s);
+int time_sigma_group_ff(kpm_ell_s* h, kpm_ell_s* v1, kpm_ell_s* v2, int R, int r0, int Rg, const double* c_u, int M2,
+                        const double* c_fd, int M, int len_t, const double* v, double* sigma, cudaStream_t s);
 // KPM_C128F: out = (sum_{m<M} c_m T_m)^steps v for one vector group (kpm_ff.cu).
 int series_group_ff(kpm_ell_s* h, int R, int r0, int Rg, int M, const double* c, int steps, const double* v,
                     double* out, cudaStream_t s);
@@ -218,6 +224,9 @@ int unpack_vectors(const void* src, bool from_f32, int64_t n, int64_t n_pad, int
                    double* dst, cudaStream_t s);
 int reduce_partials(const double2* part, int steps, int sets, int grid, int Rg, double* const* outs,
                     int R, int r0, int M, int m0, cudaStream_t s);
+// Two [n_pad][Rg] sets of 16-byte entries joined into / split from one [n_pad][2 Rg] set
+// (slots 0..Rg-1 from a, Rg..2Rg-1 from b) (kpm_capi.cu).
+int join_split(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, bool join, cudaStream_t s);
 int ensure_f32_values(kpm_ell_s* h, cudaStream_t s);
 // Profiling helpers: bracket a step loop with events when h->prof is set.
 int prof_begin(kpm_ell_s* h, cudaStream_t s, cudaEvent_t* ev);

@@ -229,15 +229,15 @@ def time_evolve(op: DeviceELL, M: int, c, steps: int, v, dtype="c128", stream=No
     return _finish(out, squeeze, was_np)
 
 
-def cheb_commutator_series(op: DeviceELL, vop: DeviceELL, M: int, c, v, stream=None):
-    """out = sum_m c[m] C_m with the commutator recursion (rec_com_A_vec)."""
+def cheb_commutator_series(op: DeviceELL, vop: DeviceELL, M: int, c, v, dtype="c128", stream=None):
+    """out = sum_m c[m] C_m with the commutator recursion (rec_com_A_vec); dtype c128 or c128f."""
     M = int(M)
     if M < 2:
         raise ValueError("M must be >= 2")
     tv, R, squeeze, was_np = _vectors(v, op.n)
     tc = _coef(c, M, tv.device)
     out = torch.empty_like(tv)
-    st = _capi.lib().kpm_cheb_commutator_series(op.handle, vop.handle, _capi.KPM_C128, R, M, tc.data_ptr(),
+    st = _capi.lib().kpm_cheb_commutator_series(op.handle, vop.handle, _capi.dtype_code(dtype), R, M, tc.data_ptr(),
                                                 tv.data_ptr(), out.data_ptr(), _stream_ptr(stream))
     _capi.check(st, "kpm_cheb_commutator_series")
     return _finish(out, squeeze, was_np)
@@ -262,13 +262,14 @@ def ell_dot(op: DeviceELL, a, b, x, y, stream=None):
     return y
 
 
-def time_sigma(op: DeviceELL, v1: DeviceELL, v2: DeviceELL, c_u, M2: int, c_fd, M: int, len_t: int, v, stream=None):
-    """sigma[r, j] = <U_c(t_j) | V1 U(t_j)> (for_time_sigma, without the -i)."""
+def time_sigma(op: DeviceELL, v1: DeviceELL, v2: DeviceELL, c_u, M2: int, c_fd, M: int, len_t: int, v,
+               dtype="c128", stream=None):
+    """sigma[r, j] = <U_c(t_j) | V1 U(t_j)> (for_time_sigma, without the -i); dtype c128 or c128f."""
     tv, R, squeeze, was_np = _vectors(v, op.n)
     tcu = _coef(c_u, int(M2), tv.device)
     tcf = _coef(c_fd, int(M), tv.device)
     sig = torch.empty((R, int(len_t)), dtype=torch.complex128, device=tv.device)
-    st = _capi.lib().kpm_time_sigma(op.handle, v1.handle, v2.handle, _capi.KPM_C128, R, tcu.data_ptr(), int(M2),
+    st = _capi.lib().kpm_time_sigma(op.handle, v1.handle, v2.handle, _capi.dtype_code(dtype), R, tcu.data_ptr(), int(M2),
                                     tcf.data_ptr(), int(M), int(len_t), tv.data_ptr(), sig.data_ptr(),
                                     _stream_ptr(stream))
     _capi.check(st, "kpm_time_sigma")

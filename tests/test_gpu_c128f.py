@@ -95,3 +95,103 @@ def test_c128f_rejects_second_moment_set(cuda_lib):
                                    mu2.data_ptr(), None)
     assert st == _capi.KPM_ERR_UNSUPPORTED
     assert isinstance(ctypes.c_int(st).value, int)
+
+
+def test_c128f_commutator_and_time_sigma_match_reference_golden(cuda_lib):
+    """The commutator series and the time-domain Kubo correlator in float-float arithmetic
+    against the reference's own outputs (rec_com_A_vec and the kpm_sigma_time loop)."""
+    from minijclsquant_gb300 import device
+
+    z = golden("honeycomb_8x8")
+    x = golden("honeycomb_8x8_more")
+    L = int(z["len_row"])
+    H = device.DeviceELL(z["data_kpm"], z["indices"], L)
+    V2 = device.DeviceELL(x["v2_data"], z["indices"], L)
+    V1 = device.DeviceELL(x["v1_data"], z["indices"], L)
+    Ms = len(x["coef"])
+    v = z["v"][0]
+    c = device.cheb_commutator_series(H, V2, Ms, x["coef"], v, dtype="c128f")
+    assert np.max(np.abs(c - x["comm"])) <= REL * np.max(np.abs(x["comm"]))
+    sig = device.time_sigma(H, V1, V2, x["cu"], int(x["M2"]), x["coef"], Ms, int(x["len_t"]), v, dtype="c128f")
+    assert np.max(np.abs(sig - x["sigma"])) <= REL * np.max(np.abs(x["sigma"]))
+
+
+@pytest.mark.parametrize("R", [1, 2, 3, 5])
+def test_c128f_time_sigma_groups_against_oracle_and_c128(cuda_lib, R):
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.kernel_and_moments import JacksonKernel, moments_FD_T0, moments_U
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity, modifier_velocity_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    H = lattice.honeycomb(20, 16, t=-2.7, W=0.8, seed=R)
+    Hk = H.modifier(modifier_bounds)
+    v1 = modifier_velocity(H, "y")
+    v2 = modifier_velocity_bounds(H, "x")
+    L = Hk.len_row
+    ops = [device.DeviceELL(d, Hk.indices, L) for d in (Hk.data, v1, v2)]
+    M, M2, len_t = 64, 12, 5
+    cu = moments_U(1.1, M2).astype(np.complex128)
+    cfd = (moments_FD_T0(0.05, M) * JacksonKernel(M)).astype(np.complex128)
+    vs = np.stack([random_vector_generator(ops[0].n, 60 + r) for r in range(R)])
+    f = np.asarray(device.time_sigma(*ops, cu, M2, cfd, M, len_t, vs, dtype="c128f")).reshape(R, len_t)
+    d = np.asarray(device.time_sigma(*ops, cu, M2, cfd, M, len_t, vs)).reshape(R, len_t)
+    for r in range(R):
+        ref = oracle.for_time_sigma(Hk.data, v1, v2, Hk.indices, L, cu, cfd, len_t, vs[r], M, M2)
+        assert np.max(np.abs(f[r] - ref)) <= REL * np.max(np.abs(ref)), r
+    assert np.max(np.abs(f - d)) <= 1e-12 * np.max(np.abs(d))
+
+
+def test_c128f_commutator_complex_hoppings_larger(cuda_lib):
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.ell_matrix import ell_matrix
+    from minijclsquant_gb300.kernel_and_moments import JacksonKernel, moments_FD_T0
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    arr = lattice.honeycomb_arrays(64, 48, t=-2.7, W=0.6, seed=12)
+    phase = np.exp(1j * 0.3 * np.real(arr["dx"]) / 0.142)
+    arr = dict(arr, data=np.where(np.real(arr["dx"]) != 0, arr["data"] * phase, arr["data"]))
+    dx = lattice.to_csr(dict(arr, data=arr["dx"]))
+    dy = lattice.to_csr(dict(arr, data=arr["dy"]))
+    H = ell_matrix(lattice.to_csr(arr), dx, dy)
+    Hk = H.modifier(modifier_bounds)
+    V = modifier_velocity_bounds(H, "x")
+    L = Hk.len_row
+    hop = device.DeviceELL(Hk.data, Hk.indices, L)
+    vop = device.DeviceELL(V, Hk.indices, L)
+    M = 200
+    c = (moments_FD_T0(-0.2, M) * JacksonKernel(M)).astype(np.complex128)
+    vs = np.stack([random_vector_generator(hop.n, 7 + r) for r in range(4)])
+    out = np.asarray(device.cheb_commutator_series(hop, vop, M, c, vs, dtype="c128f"))
+    for r in range(4):
+        ref = oracle.rec_com_A_vec(M, Hk.data, V, Hk.indices, L, c, vs[r])
+        assert np.max(np.abs(out[r] - ref)) <= REL * np.max(np.abs(ref)), r
+
+
+def test_c128f_commutator_and_time_sigma_on_reused_handles(cuda_lib):
+    """Workspace reuse: the commutator recursion reads C_0 = 0 from a scratch buffer that an
+    earlier call (of either precision) left filled; repeated calls on the same handles and a
+    float-float call after an FP64 one return the oracle's values."""
+    from minijclsquant_gb300 import device, lattice
+    from minijclsquant_gb300.kernel_and_moments import JacksonKernel, moments_FD_T0, moments_U
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity, modifier_velocity_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    H = lattice.honeycomb(20, 16, t=-2.7, W=0.8, seed=3)
+    Hk = H.modifier(modifier_bounds)
+    v1, v2 = modifier_velocity(H, "y"), modifier_velocity_bounds(H, "x")
+    L = Hk.len_row
+    ops = [device.DeviceELL(d, Hk.indices, L) for d in (Hk.data, v1, v2)]
+    M, M2, len_t = 64, 12, 4
+    cu = moments_U(1.1, M2).astype(np.complex128)
+    cfd = (moments_FD_T0(0.05, M) * JacksonKernel(M)).astype(np.complex128)
+    vs = np.stack([random_vector_generator(ops[0].n, 60 + r) for r in range(3)])
+    sig_ref = [oracle.for_time_sigma(Hk.data, v1, v2, Hk.indices, L, cu, cfd, len_t, vs[r], M, M2) for r in range(3)]
+    com_ref = [oracle.rec_com_A_vec(M, Hk.data, v2, Hk.indices, L, cfd, vs[r]) for r in range(3)]
+    for dtypes in (("c128", "c128f"), ("c128f", "c128f")):
+        for dt in dtypes:
+            s = np.asarray(device.time_sigma(*ops, cu, M2, cfd, M, len_t, vs, dtype=dt)).reshape(3, len_t)
+            c = np.asarray(device.cheb_commutator_series(ops[0], ops[2], M, cfd, vs, dtype=dt))
+            for r in range(3):
+                assert np.max(np.abs(s[r] - sig_ref[r])) <= REL * np.max(np.abs(sig_ref[r])), (dt, r)
+                assert np.max(np.abs(c[r] - com_ref[r])) <= REL * np.max(np.abs(com_ref[r])), (dt, r)

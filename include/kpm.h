@@ -51,7 +51,8 @@ extern "C" {
 #define KPM_C64 1    /* complex64 recursion and values, FP64 moment accumulation */
 #define KPM_C128F 2  /* complex128 accuracy in float-float arithmetic on the FP32 pipe
                         (kpm_cheb_moments without mu_rr, kpm_cheb_series,
-                        kpm_time_evolve; see kpm_cheb_moments)                     */
+                        kpm_time_evolve, kpm_cheb_commutator_series,
+                        kpm_time_sigma, kpm_adjoint_backward_ex; see kpm_cheb_moments) */
 
 /* ---- operator creation flags ------------------------------------------- */
 #define KPM_FLAG_DEVICE_PTRS 1u   /* data/indices are device pointers        */
@@ -174,6 +175,8 @@ int kpm_time_evolve(kpm_ell* h, int dtype, int R, int M, const double* c, int st
  * C_m = 2 H C_{m-1} - C_{m-2} + 2 V T_{m-1}.  H and V are separate operators
  * of equal size.  Replaces rec_com_A_vec (jclsquant/recurrence_functions.py:146-196;
  * jclsquant/cuda_cython/cuda/recursions.cu:319-388).
+ * dtype KPM_C128 or KPM_C128F (the recursion and the series in float pairs,
+ * H and V read as float pairs; the result unpacked to complex128).
  */
 int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M,
                                const double* c, const double* v, double* out, void* stream);
@@ -185,6 +188,9 @@ int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int 
  * The caller multiplies by -i as jclsquant/observables_gpu.py does.
  * c_u: device [M2] c128; c_fd: device [M] c128; v: device [R][n]; sigma: device [R][len_t].
  * Replaces for_time_sigma (jclsquant/cuda_cython/cuda/obv.cu:124-176).
+ * dtype KPM_C128, or KPM_C128F: U and U_c stay in float pairs on the device for
+ * all len_t steps (commutator series, series steps and the V1 products in float
+ * pairs); each sigma[r][j] is reduced in FP64.
  */
 int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u,
                    int M2, const double* c_fd, int M, int len_t, const double* v,

@@ -83,20 +83,23 @@ __global__ void light_kernel(int64_t count, double2 a, double2 kx, double2 ky, c
   }
 }
 
-// H(t) into the doubled SoA values of an operator.  Threads walk the reference-layout
-// inputs in order (k = row * L + s: coalesced reads); the eight consecutive rows a warp
-// covers in each slot plane s * n_pad + row are whole 128-byte segments of the output.
-// The padding rows (row >= n) keep the zeros written at creation.
+// H(t) into the doubled SoA values of an operator, one thread per row.  Every lane runs
+// the same slot loop, so a slot whose phase argument is zero on the whole warp (the
+// on-site and padding slots: dx = dy = 0) skips the FP64 sincos together: exp(0) = 1
+// exactly.  Stores are whole 128-byte segments of each slot plane s * n_pad + row; the
+// row's L consecutive inputs come through L1.  Padding rows (row >= n) keep the zeros
+// written at creation.
 __global__ void light_update_kernel(int64_t n, int64_t n_pad, int L, double2 a, double2 kx, double2 ky,
                                     const double2* __restrict__ data, const double2* __restrict__ dx,
                                     const double2* __restrict__ dy, double2* __restrict__ val) {
-  const int64_t total = n * L;
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t row = k / L;
-    const int s = (int)(k - row * L);
-    const double2 z = cadd(cmul(kx, dx[k]), cmul(ky, dy[k]));
-    const double2 v = cmul(cmul(a, data[k]), cexp2(z));
-    val[(int64_t)s * n_pad + row] = make_double2(2.0 * v.x, 2.0 * v.y);
+  for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
+    for (int s = 0; s < L; ++s) {
+      const int64_t k = row * L + s;
+      const double2 z = cadd(cmul(kx, dx[k]), cmul(ky, dy[k]));
+      const double2 e = (z.x == 0.0 && z.y == 0.0) ? make_double2(1.0, 0.0) : cexp2(z);
+      const double2 v = cmul(cmul(a, data[k]), e);
+      val[(int64_t)s * n_pad + row] = make_double2(2.0 * v.x, 2.0 * v.y);
+    }
   }
 }
 
@@ -166,7 +169,7 @@ int kpm_ell_light_update(kpm_ell* h, const double* params, const double* data0, 
   double2 a, kx, ky;
   light_coefficients(params, &a, &kx, &ky);
   cudaStream_t s = stream_of(stream);
-  light_update_kernel<<<grid_for_count(h->n * (int64_t)h->L), 256, 0, s>>>(
+  light_update_kernel<<<grid_for_count(h->n), 256, 0, s>>>(
       h->n, h->n_pad, h->L, a, kx, ky, reinterpret_cast<const double2*>(data0), reinterpret_cast<const double2*>(dx),
       reinterpret_cast<const double2*>(dy), static_cast<double2*>(h->val64));
   KPM_TRY(check_cuda(cudaGetLastError()));

@@ -32,14 +32,15 @@ def kpm_dos_2_gpu(H, M=None, random_vector_l=None, random_vector_r=None, bounds=
 
 
 def kpm_sigma_time_gpu(H, direction_1=None, direction_2=None, t_vec=None, Ef=None, Temp=None, M=None,
-                       random_vector=None, velocities=None):
+                       random_vector=None, velocities=None, *, dtype="c128"):
     """Time-dependent Kubo conductivity correlator -i <U_c(t)|V1 U(t)>.
 
     Follows kpm_sigma_time_gpu of jclsquant's observables_gpu (historical
     version, .history/jclsquant/observables_gpu_20260306165252.py:103-175):
     Bessel moments truncated where |c_m| <= 1e-15, Fermi-Dirac moments times
     Jackson, V2 = H o d / a (rescaled), V1 = -i H o d, and the GPU
-    for_time_sigma recursion.
+    for_time_sigma recursion.  ``dtype="c128f"`` runs the recursion in float-float
+    arithmetic (about 48-bit mantissas) on the FP32 pipe.
     """
     if M is None:
         M = int(np.sqrt(H.shape[0]))
@@ -73,5 +74,5 @@ def kpm_sigma_time_gpu(H, direction_1=None, direction_2=None, t_vec=None, Ef=Non
         V1.data = np.copy(d1)
         V2_kpm.data = (1j / ((H.bounds[1] - H.bounds[0]) / 2)) * d2 + 0 * V2_kpm.data
     sigma = device.time_sigma(H_kpm.device(), V1.device(), V2_kpm.device(), mu_u.astype(np.complex128), M2, mk_fd, M,
-                              len(t_vec), np.asarray(random_vector, dtype=np.complex128))
+                              len(t_vec), np.asarray(random_vector, dtype=np.complex128), dtype=dtype)
     return -1j * sigma

@@ -195,3 +195,36 @@ def test_c128f_commutator_and_time_sigma_on_reused_handles(cuda_lib):
             for r in range(3):
                 assert np.max(np.abs(s[r] - sig_ref[r])) <= REL * np.max(np.abs(sig_ref[r])), (dt, r)
                 assert np.max(np.abs(c[r] - com_ref[r])) <= REL * np.max(np.abs(com_ref[r])), (dt, r)
+
+
+def test_kpm_sigma_time_gpu_both_precisions(cuda_lib):
+    """The observable drop-in (kpm_sigma_time_gpu of jclsquant's observables_gpu): its c128
+    result equals -i times the oracle's for_time_sigma on the moments it builds, and the
+    float-float run agrees with it."""
+    from minijclsquant_gb300 import lattice
+    from minijclsquant_gb300.constants import hbar_fs
+    from minijclsquant_gb300.kernel_and_moments import JacksonKernel, moments_FD_T0, moments_U
+    from minijclsquant_gb300.modifiers import modifier_bounds, modifier_velocity, modifier_velocity_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+    from minijclsquant_gb300.observables_gpu import kpm_sigma_time_gpu
+
+    H = lattice.honeycomb(14, 12, t=-2.7, W=0.6, seed=4)
+    n = H.shape[0]
+    v = random_vector_generator(n, 21)
+    M, Ef = 96, 0.3
+    t_vec = np.linspace(0, 4.0, 7)
+    sig = kpm_sigma_time_gpu(H, "x", "y", t_vec=t_vec, Ef=Ef, M=M, random_vector=v)
+    sig_f = kpm_sigma_time_gpu(H, "x", "y", t_vec=t_vec, Ef=Ef, M=M, random_vector=v, dtype="c128f")
+    dt = t_vec[1] * H.bounds[1] / hbar_fs
+    mu_u = moments_U(dt, M)
+    M2 = 0
+    while np.abs(mu_u[M2]) > 1e-15 and M2 < M - 1:
+        M2 += 1
+    cu = moments_U(dt, M2).astype(np.complex128)
+    cfd = (moments_FD_T0(Ef / H.bounds[1], M) * JacksonKernel(M)).astype(np.complex128)
+    Hk = H.modifier(modifier_bounds)
+    ref = -1j * oracle.for_time_sigma(Hk.data, H.modifier(modifier_velocity, "x").data,
+                                      H.modifier(modifier_velocity_bounds, "y").data, Hk.indices, Hk.len_row, cu, cfd,
+                                      len(t_vec), v, M, M2)
+    assert np.max(np.abs(sig - ref)) <= REL * np.max(np.abs(ref))
+    assert np.max(np.abs(sig_f - sig)) <= REL * np.max(np.abs(sig))

@@ -139,8 +139,16 @@ static bool same_shape(const TunedShape& t, const kpm_ell_s* h, int key) {
          t.structure == h->structure;
 }
 
+bool ff_moment_products(bool f32, int sets) {
+  if (f32 || sets != 1) return false;
+  const char* e = getenv("KPM_MOMENTS_FP64");
+  return !(e && *e && std::string(e) != "0");
+}
+
 int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepConfig* out) {
-  const int key = (f32 ? 1000 : 0) + Rg * 10 + sets;
+  // FP64 one-set moments: the producer-warp candidates are timed with float-float products
+  const bool ffm = ff_moment_products(f32, sets);
+  const int key = (f32 ? 1000 : 0) + (ffm ? 100 : 0) + Rg * 10 + sets;
   for (auto& kv : h->tuned)
     if (kv.first == key) {
       *out = kv.second;
@@ -212,6 +220,10 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
     p.dbl = sets == 3;
     p.hv = sets == 3 ? ws.vr.p : nullptr;
     p.part = static_cast<double2*>(ws.part.p);
+    if (ffm) {  // zeros read as float pairs: every element on the float-float path
+      p.vl_ff = 1;
+      p.vl64 = ws.vl.p;
+    }
     if (sets == 4) {  // series into ws.vl with a zero coefficient
       p.series = ws.vl.p;
       p.coef = static_cast<const double2*>(ws.part.p);
@@ -602,6 +614,14 @@ int moments_group(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const do
   p.tout = ws.tb.p;
   p.part = part;
   KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_FIRST, EPI_STORE | EPI_MOM1, p, grid, s));
+  if (M > 2 && cfg.kind == 2 && ff_moment_products(f32, sets)) {
+    // later steps: FP64 recursion, moment products in float-float arithmetic
+    KPM_TRY(ensure(ws.vf, (size_t)h->n_pad * Rg * sizeof(float4)));
+    KPM_TRY(pack_left_ff(v_l ? v_l : v_r, h->n, h->n_pad, R, r0, Rg, ws.vf.p, s));
+    p.vl64 = ws.vl.p;
+    p.vl = ws.vf.p;
+    p.vl_ff = 1;
+  }
   void* tprev = ws.ta.p;  // T_{m-2}
   void* tcur = ws.tb.p;   // T_{m-1}
   int m0 = 0;

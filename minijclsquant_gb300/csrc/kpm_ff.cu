@@ -700,6 +700,43 @@ int ff_corr_launch(bool rv, int R, const kpm_ell_s* v1, const float4* u, const f
 
 }  // namespace
 
+// Left vectors for float-float moment products of the FP64 recursion: complex128 [R][n] ->
+// float pairs [n_pad][Rg] (hi = the nearest float, lo = the nearest float to the rest).  A
+// component that is neither zero nor in [2^-50, 2^61) gets a NaN high part, which sends
+// that element to the FP64 product (ff_left_ok).
+__global__ void pack_left_ff_kernel(const double2* __restrict__ src, int64_t n, int64_t n_pad, int R, int r0, int Rg,
+                                    float4* __restrict__ dst) {
+  const int64_t total = n_pad * Rg;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = t / Rg;
+    const int r = (int)(t % Rg);
+    double2 z = make_double2(0.0, 0.0);
+    if (row < n) z = src[(int64_t)(r0 + r) * n + row];
+    float q[4];
+    const double c[2] = {z.x, z.y};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const double a = fabs(c[k]);
+      if (c[k] == 0.0 || (a >= 0x1p-50 && a < 0x1p61)) {
+        q[k] = (float)c[k];
+        q[k + 2] = (float)(c[k] - (double)q[k]);
+      } else {
+        q[k] = __uint_as_float(0x7fffffffu);
+        q[k + 2] = 0.f;
+      }
+    }
+    dst[t] = make_float4(q[0], q[1], q[2], q[3]);
+  }
+}
+
+int pack_left_ff(const double* v, int64_t n, int64_t n_pad, int R, int r0, int Rg, void* dst, cudaStream_t s) {
+  const int64_t total = n_pad * Rg;
+  const int pg = (int)std::min<int64_t>((total + 255) / 256, 65536);
+  pack_left_ff_kernel<<<pg, 256, 0, s>>>(reinterpret_cast<const double2*>(v), n, n_pad, R, r0, Rg,
+                                         static_cast<float4*>(dst));
+  return check_cuda(cudaGetLastError());
+}
+
 // Commutator series (rec_com_A_vec) of vectors r0 .. r0 + Rg in float-float arithmetic.
 int comm_series_group_ff(kpm_ell_s* h, kpm_ell_s* v, int R, int r0, int Rg, int M, const double* c, const double* x,
                          double* out, cudaStream_t s) {

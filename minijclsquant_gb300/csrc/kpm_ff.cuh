@@ -74,6 +74,59 @@ __device__ __forceinline__ void ff_fold(double& re, double& im, FFMom& m) {
   m = FFMom{0.f, 0.f, 0.f, 0.f};
 }
 
+// ---- FP64 recursion with float-float moment products -------------------------------
+// The FP64 vector T_{m+1} is split into float pairs with integer operations only (the FP64
+// pipe, the bound of the FP64 recursion, does no extra work): hi is x rounded to 24
+// significant bits (an integer add of half the dropped unit carries into the exponent
+// when it must), lo = x - hi exactly as a signed 29-bit count of x's last-place units,
+// rounded to a float, so hi + lo = x to 2^-49 relative.  The left vector is packed once
+// per call (pack_left_ff).  Products run through ff_cdot, and the float-pair sums are
+// folded into FP64 every kFfFoldRows rows.  A value outside [2^-50, 2^61) that is not zero
+// (nor an FP64 subnormal, taken as zero) reports false, and the caller forms that row's
+// product in FP64 instead: every float-pair product and its rounding error then stay
+// normal floats.
+constexpr int kFfFoldRows = 32;
+
+__device__ __forceinline__ bool ff_split_f64(double x, float& hi, float& lo) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long r = b + (1ull << 28);  // round the 29 dropped bits to nearest
+  const unsigned hb = (unsigned)(b >> 32), lb = (unsigned)b;
+  const unsigned rh = (unsigned)(r >> 32), rlw = (unsigned)r & 0xe0000000u;
+  const unsigned sgn = hb & 0x80000000u;
+  const unsigned e = (hb >> 20) & 0x7ffu;
+  const unsigned er = (rh >> 20) & 0x7ffu;  // e or e + 1
+  const bool normal = e >= 973u;
+  // float exponent field er - 896 (= er - 1023 + 127); 20 + 3 mantissa bits
+  hi = __uint_as_float(normal ? (sgn | ((er - 896u) << 23) | ((rh & 0xfffffu) << 3) | (rlw >> 29)) : 0u);
+  // |x| - |hi| = d 2^(e - 1075): d the low words' difference, within [-2^28, 2^28].  d is
+  // converted without a conversion instruction (those issue on the FP64 pipe): for |k| < 2^22,
+  // bits(1.5 2^(23+s)) + k read as a float is 1.5 2^(23+s) + k 2^s exactly, so subtracting
+  // the constant leaves k 2^s.  d = dh 2^14 + dl with dh (signed) and dl in [0, 2^14).
+  const int d = (int)(lb - rlw);
+  const unsigned ch = normal ? (((e - 911u) << 23) | 0x400000u) : 0u;  // 1.5 2^(23 + e - 1061)
+  const unsigned cl = normal ? (((e - 925u) << 23) | 0x400000u) : 0u;  // 1.5 2^(23 + e - 1075)
+  const float fh = __fsub_rn(__uint_as_float(ch + (unsigned)(d >> 14)), __uint_as_float(ch));
+  const float fl = __fsub_rn(__uint_as_float(cl + (unsigned)(d & 0x3fff)), __uint_as_float(cl));
+  lo = normal ? __uint_as_float(__float_as_uint(__fadd_rn(fh, fl)) ^ sgn) : 0.f;
+  return e == 0u || (normal && e <= 1083u);
+}
+
+// a packed left-vector high part: zero, or a normal float in [2^-50, 2^61) (NaN marks an
+// element that pack_left_ff could not carry)
+__device__ __forceinline__ bool ff_left_ok(float h) {
+  const unsigned u = __float_as_uint(h) & 0x7fffffffu;
+  const unsigned ef = u >> 23;
+  return u == 0u || (ef >= 77u && ef <= 187u);
+}
+
+// the float pairs of a packed left-vector entry carried in a double2 slot
+__device__ __forceinline__ FF ff_from_slot(double re, double im) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(re);
+  const unsigned long long b = (unsigned long long)__double_as_longlong(im);
+  return FF{__uint_as_float((unsigned)a), __uint_as_float((unsigned)(a >> 32)), __uint_as_float((unsigned)b),
+            __uint_as_float((unsigned)(b >> 32))};
+}
+
 template <bool REAL>
 struct FFVal { using type = float2; };
 template <>

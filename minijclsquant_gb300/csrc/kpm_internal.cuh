@@ -72,6 +72,7 @@ struct Workspace {
   DevBuf coef;             // small device staging (coefficients)
   DevBuf ckpt, seg, grad;  // adjoint: checkpoint pairs, recomputed segment, per-slot gradient
   DevBuf red;              // doubling: reduced sets [2][R][K + 1], then the per-vector corrections
+  DevBuf vf;               // float-pair left vectors of the FP64 recursion's moment products
 };
 
 // Kernel choice for the recursion step of one (precision, R group, moment sets).
@@ -151,6 +152,10 @@ struct StepParams {
   int dbl;
   const void* hv;         // dbl: |v|^2 / 2, real, [n_pad][R] (working precision)
   int64_t part_set_stride;  // per_tile with two sets: elements between the sets' slot blocks
+  // FP64 recursion with float-float moment products (producer-warp kernel, one moment
+  // set): vl holds the float pairs of pack_left_ff, vl64 the same vectors in FP64
+  int vl_ff;
+  const void* vl64;
 };
 
 // Launch helpers implemented per precision (kpm_cheb_c128.cu, kpm_cheb_c64.cu).
@@ -227,6 +232,12 @@ int reduce_partials(const double2* part, int steps, int sets, int grid, int Rg, 
 // Two [n_pad][Rg] sets of 16-byte entries joined into / split from one [n_pad][2 Rg] set
 // (slots 0..Rg-1 from a, Rg..2Rg-1 from b) (kpm_capi.cu).
 int join_split(double2* a, double2* b, double2* both, int64_t n_pad, int Rg, bool join, cudaStream_t s);
+// Float pairs of the left vectors r0 .. r0 + Rg for the FP64 recursion's float-float moment
+// products ([n_pad][Rg] float4; kpm_ff.cu).
+int pack_left_ff(const double* v, int64_t n, int64_t n_pad, int R, int r0, int Rg, void* dst, cudaStream_t s);
+// FP64 one-set moments form their products in float-float arithmetic (producer-warp
+// kernel) unless KPM_MOMENTS_FP64 is set to a nonzero value.
+bool ff_moment_products(bool f32, int sets);
 int ensure_f32_values(kpm_ell_s* h, cudaStream_t s);
 // Profiling helpers: bracket a step loop with events when h->prof is set.
 int prof_begin(kpm_ell_s* h, cudaStream_t s, cudaEvent_t* ev);

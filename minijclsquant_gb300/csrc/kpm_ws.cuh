@@ -24,12 +24,18 @@
 // vector and the two moment sets <T_{m+1}|T_m>, sum (|T_m|^2 - |v|^2 / 2) are
 // accumulated (T_m's own row read from tcur).
 //
+// With p.vl_ff (FP64 only, one moment set) the staged left vector holds float pairs and the
+// moment products run in float-float arithmetic on the FP32 pipe (ff_split_f64 / ff_cdot,
+// folded into FP64 every kFfFoldRows rows); an element outside the float-pair range takes
+// the FP64 product with v_l read from p.vl64.  The recursion itself stays FP64.
+//
 // Every wait is bounded.  A compute warp whose wait runs out records
 // KPM_ERR_TIMEOUT and stops computing but still takes part in the named
 // barriers, so no warp waits on one that has left; the producer that times
 // out stops issuing and waits (bounded) for its copies in flight before exit.
 #pragma once
 
+#include "kpm_ff.cuh"
 #include "kpm_staged.cuh"
 
 namespace kpm {
@@ -38,7 +44,7 @@ constexpr int kWsStages = 4;
 constexpr int kWsThreads = kBlock + 32;  // compute warps + one producer warp
 
 template <typename T, bool REAL, int TPR, int VPT, int U, bool SER>
-__global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_kernel(const StepParams p) {
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && TPR >= 2) ? 3 : 2) : 1)) cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;
   constexpr int R = TPR * VPT;
@@ -140,6 +146,11 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
   }
   int pending = 0;
   bool dead = false;
+  // FP64 recursion, float-float moment products
+  const bool vlff = !F32 && VPT == 1 && p.vl_ff != 0 && !dbl;
+  const double2* __restrict__ vl64 = static_cast<const double2*>(p.vl64);
+  FFMom fm{0.f, 0.f, 0.f, 0.f};
+  int ffp = 0;
   auto fold = [&]() {
 #pragma unroll
     for (int q = 0; q < VPT; ++q) {
@@ -150,6 +161,10 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
     }
   };
   auto flush_sets = [&](double2* dst) {
+    if (vlff) {
+      ff_fold(mr[0], mi[0], fm);
+      ffp = 0;
+    }
     block_reduce_store<TPR, VPT>(mr, mi, dst, red, true);
     if (dbl) block_reduce_store<TPR, VPT>(mr2, mi2, dst + set_stride, red, true);
 #pragma unroll
@@ -246,6 +261,24 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? 2 : 1)) cheb_next_ws_ker
             } else {
               cdot_acc(mr[q], mi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
               mr2[q] += fma(own.re[q], own.re[q], fma(own.im[q], own.im[q], -hvs[u][q]));
+            }
+          }
+        } else if (vlff) {
+          if constexpr (!F32) {
+            const FF lf = ff_from_slot(l[u].re[0], l[u].im[0]);
+            FF tf;
+            bool ok = ff_split_f64(acc[u].re[0], tf.rh, tf.rl);
+            ok &= ff_split_f64(acc[u].im[0], tf.ih, tf.il);
+            ok &= ff_left_ok(lf.rh) & ff_left_ok(lf.ih);
+            if (ok) {
+              ff_cdot(fm, lf, tf);
+            } else {
+              const double2 lv = __ldg(vl64 + vi);
+              cdot_acc(mr[0], mi[0], lv.x, lv.y, acc[u].re[0], acc[u].im[0]);
+            }
+            if (++ffp == kFfFoldRows) {
+              ffp = 0;
+              ff_fold(mr[0], mi[0], fm);
             }
           }
         } else {

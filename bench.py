@@ -1007,12 +1007,20 @@ def run_ours(a):
                 "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_launch_s * 1e3}
     fma_rate = ctypes.c_double()
     _capi.check(lib.kpm_measure_fp64_fma_rate(ctypes.byref(fma_rate), ctypes.c_void_p(int(stream.cuda_stream))))
-    fma_per_site_step = (2 * L if op.is_real else 4 * L) + (6 if doubled else 4)
+    # FP64 FMAs per site-step: the recursion's 2L (real values) or 4L, plus the moment's 4 unless
+    # the producer-warp kernel forms the moment products in float-float arithmetic (the default
+    # for one moment set; KPM_MOMENTS_FP64=1 turns it off)
+    ff_products = (a.dtype == "c128" and not doubled and kind.value == 2
+                   and os.environ.get("KPM_MOMENTS_FP64", "") in ("", "0"))
+    rec_fma = 2 * L if op.is_real else 4 * L
+    fma_per_site_step = rec_fma + (6 if doubled else (0 if ff_products else 4))
     fp64 = None
     if a.dtype == "c128":
         ach = fma_per_site_step * float(n) * R / avg_launch_s
         fp64 = {"achieved_fma_per_s": ach, "peak_fma_per_s": fma_rate.value, "frac": ach / fma_rate.value,
-                "fma_per_site_step": fma_per_site_step, "peak_source": "measured live (independent FP64 FMA chains)"}
+                "fma_per_site_step": fma_per_site_step, "peak_source": "measured live (independent FP64 FMA chains)",
+                "moment_products": ("float-float on the FP32 pipe (2^-49 per product), FP64 sums" if ff_products
+                                    else "FP64")}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": ms_max / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -1042,7 +1050,7 @@ def run_ours(a):
         line["doubling"] = {
             "value": float(n) * R * (M - 1) * world / (ms_d * 1e-3), "ms_per_step": ms_d,
             "executed_steps_per_recursion": executed_steps(M, True) + 1, "moments_per_recursion": M,
-            "fma_per_executed_site_step": fma_per_site_step + 2,
+            "fma_per_executed_site_step": rec_fma + 6,
             "max_abs_diff_vs_direct_over_mu0": float(np.max(np.abs(mu_dbl.cpu().numpy() - mu_h))
                                                      / np.max(np.abs(mu_h[:, 0]))),
             "note": "opt-in (KPM_FLAG_DOUBLING); value counts site-steps per moment delivered, N R (M-1)"}

@@ -96,10 +96,13 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
   // tiles of this CTA: strided (plain operators) or one contiguous range (batched)
   const int seg_tb = (int)(((int64_t)blockIdx.x * ntiles) / gridDim.x);
   const int seg_te = (int)(((int64_t)(blockIdx.x + 1) * ntiles) / gridDim.x);
-  const int my_count = p.per_tile ? seg_te - seg_tb
+  // kernel-parameter fields read in the tile loop are copied to registers first (a
+  // reference to p taken by a lambda would place p in local memory)
+  const bool per_tile = p.per_tile != 0;
+  const int my_count = per_tile ? seg_te - seg_tb
                                   : (((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0);
-  auto tile_of = [&](int k) -> int64_t {
-    return p.per_tile ? (int64_t)seg_tb + k : (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
+  auto tile_of = [per_tile, seg_tb](int k) -> int64_t {
+    return per_tile ? (int64_t)seg_tb + k : (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
   };
 
   if (threadIdx.x == 0) {
@@ -131,8 +134,8 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
       issue_tile(tc, smem + (k % kStages) * stage_b, &bars[k % kStages], tile_of(k) * TILE, TPR * (int)sizeof(Raw),
                  pol);
   }
-  int seg = p.per_tile ? p.seg_base[blockIdx.x] : 0;
-  int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
+  int seg = per_tile ? p.seg_base[blockIdx.x] : 0;
+  int cur_inst = (per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
 
   const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
   Raw* tout = static_cast<Raw*>(p.tout);
@@ -232,7 +235,7 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
       }
       return;
     }
-    if (p.per_tile) {
+    if (per_tile) {
       // flush the accumulators when the next tile belongs to another instance (or at the end)
       const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
       if (next_inst != cur_inst) {
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
     }
   }
 
-  if (!p.per_tile) {
+  if (!per_tile) {
     if (F32) {
 #pragma unroll
       for (int q = 0; q < VPT; ++q) {

@@ -68,10 +68,13 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   const int ntiles = (int)(p.n_pad / TILE);
   const int seg_tb = (int)(((int64_t)blockIdx.x * ntiles) / gridDim.x);
   const int seg_te = (int)(((int64_t)(blockIdx.x + 1) * ntiles) / gridDim.x);
-  const int my_count = p.per_tile ? seg_te - seg_tb
+  // kernel-parameter fields read in the tile loop are copied to registers first (a
+  // reference to p taken by a lambda would place p in local memory)
+  const bool per_tile = p.per_tile != 0;
+  const int my_count = per_tile ? seg_te - seg_tb
                                   : (((int)blockIdx.x < ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0);
-  auto tile_of = [&](int k) -> int64_t {
-    return p.per_tile ? (int64_t)seg_tb + k : (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
+  auto tile_of = [per_tile, seg_tb](int k) -> int64_t {
+    return per_tile ? (int64_t)seg_tb + k : (int64_t)blockIdx.x + (int64_t)k * gridDim.x;
   };
 
   if (threadIdx.x == 0) {
@@ -123,15 +126,15 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
     return;
   }
 
-  int seg = p.per_tile ? p.seg_base[blockIdx.x] : 0;
-  int cur_inst = (p.per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
+  int seg = per_tile ? p.seg_base[blockIdx.x] : 0;
+  int cur_inst = (per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
   const bool dbl = p.dbl != 0;
   const bool mom = p.vl != nullptr || dbl;
   // series step: series += c_m T_{m+1} (rec_A_vec), the accumulator tile staged like v_l
   constexpr bool ser = SER;
   Raw* series = static_cast<Raw*>(p.series);
   const double2 cm = ser ? p.coef[p.m] : make_double2(0.0, 0.0);
-  const int64_t set_stride = p.per_tile ? p.part_set_stride : (int64_t)gridDim.x * R;
+  const int64_t set_stride = per_tile ? p.part_set_stride : (int64_t)gridDim.x * R;
 
   const Raw* __restrict__ tcur = static_cast<const Raw*>(p.tcur);
   Raw* tout = static_cast<Raw*>(p.tout);
@@ -296,7 +299,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
         }
       }
     }
-    if (p.per_tile && mom) {
+    if (per_tile && mom) {
       const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
       if (next_inst != cur_inst) {
         if (F32) {
@@ -310,7 +313,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
     }
   }
 
-  if (!p.per_tile && mom) {
+  if (!per_tile && mom) {
     if (F32) fold();
     flush_sets(p.part + (int64_t)blockIdx.x * R);
   }

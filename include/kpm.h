@@ -47,7 +47,8 @@ extern "C" {
 #define KPM_ERR_TOO_LARGE 10    /* beyond the fixed scratch of kpm_cheb_moments_noalloc */
 
 /* ---- precision selectors ----------------------------------------------- */
-#define KPM_C128 0   /* complex128 recursion, FP64 moments (the drop-in form)   */
+#define KPM_C128 0   /* complex128 recursion, FP64 moments (the drop-in form;
+                        see kpm_cheb_moments for the arithmetic of the products) */
 #define KPM_C64 1    /* complex64 recursion and values, FP64 moment accumulation */
 #define KPM_C128F 2  /* complex128 accuracy in float-float arithmetic on the FP32 pipe
                         (kpm_cheb_moments without mu_rr, kpm_cheb_series,
@@ -142,6 +143,14 @@ int kpm_ell_dot(kpm_ell* h, double a_re, double a_im, double b_re, double b_im,
  */
 int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r,
                      const double* v_l, double* mu, double* mu_rr, void* stream);
+/* dtype KPM_C128 arithmetic: the recursion is FP64 throughout.  With one moment set
+ * (mu_rr NULL, no doubling) on the producer-warp step kernel, the products
+ * conj(v_l) T_m are formed in float-float arithmetic: each FP64 element is split exactly
+ * into a float pair to 2^-49, products use TwoProduct, and the sums are FP64.  That
+ * frees the FP64 pipe, the bound of this step on GB300.  An element that is neither
+ * zero nor in [2^-50, 2^61) takes the FP64 product.  Per order the moments are within
+ * 2e-11 of all-FP64 products, relative to max(|mu_m|, 1e-6 |mu_0|).  Setting
+ * KPM_MOMENTS_FP64=1 in the environment keeps every product in FP64. */
 /* dtype KPM_C128F: the same moments with every real number carried as a pair of
  * floats (~48 significant bits; exact products and sums), so the recursion runs on
  * the FP32 pipe -- GB300's FP64 rate is 1/64 of its FP32 rate -- with the memory

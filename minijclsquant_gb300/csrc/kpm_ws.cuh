@@ -11,7 +11,7 @@
 // neighbour gathers T_m[col] the others compute, and the producer refills a
 // stage as soon as the last warp has left it.
 //
-// The SER instantiation is a series step of rec_A_vec (p.series set, p.vl null, no
+// The series instantiation (K = kWsSeries) is a series step of rec_A_vec (p.series set, p.vl null, no
 // doubling): the producer stages the series accumulator tile in the left-vector
 // slot and the compute warps write back series + c_m T_{m+1}; no moments are formed.
 //
@@ -24,10 +24,11 @@
 // vector and the two moment sets <T_{m+1}|T_m>, sum (|T_m|^2 - |v|^2 / 2) are
 // accumulated (T_m's own row read from tcur).
 //
-// With p.vl_ff (FP64 only, one moment set) the staged left vector holds float pairs and the
-// moment products run in float-float arithmetic on the FP32 pipe (ff_split_f64 / ff_cdot,
-// folded into FP64 every kFfFoldRows rows); an element outside the float-pair range takes
-// the FP64 product with v_l read from p.vl64.  The recursion itself stays FP64.
+// With p.vl_ff (FP64 only, one moment set; K = kWsFF) the staged left vector holds float
+// pairs and the moment products run in float-float arithmetic on the FP32 pipe
+// (ff_split_f64 / ff_cdot, folded into FP64 every kFfFoldRows rows); an element outside the
+// float-pair range takes the FP64 product with v_l read from p.vl64.  The recursion itself
+// stays FP64.
 //
 // Every wait is bounded.  A compute warp whose wait runs out records
 // KPM_ERR_TIMEOUT and stops computing but still takes part in the named
@@ -43,14 +44,22 @@ namespace kpm {
 constexpr int kWsStages = 4;
 constexpr int kWsThreads = kBlock + 32;  // compute warps + one producer warp
 
-template <typename T, bool REAL, int TPR, int VPT, int U, bool SER>
-__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && TPR >= 2) ? 3 : 2) : 1)) cheb_next_ws_kernel(const StepParams p) {
+// Epilogue variants (template parameter K): each instantiation carries only its own code, so
+// the registers of one do not limit the occupancy of another.
+constexpr int kWsMom = 0;     // FP64 / complex64 moments (one set or doubled), or store only
+constexpr int kWsSeries = 1;  // series step
+constexpr int kWsFF = 2;      // FP64 recursion, one moment set with float-float products
+
+template <typename T, bool REAL, int TPR, int VPT, int U, int K>
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && TPR >= 2) ? 3 : 2) : 1))
+    cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;
   constexpr int R = TPR * VPT;
   constexpr int RPB = kBlock / TPR;
   constexpr int TILE = RPB * U;
   constexpr bool F32 = std::is_same<T, float>::value;
+  constexpr bool SER = K == kWsSeries;
   constexpr int kFlush = 8;
   constexpr int kWarps = kBlock / 32;
 
@@ -128,7 +137,9 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
 
   int seg = per_tile ? p.seg_base[blockIdx.x] : 0;
   int cur_inst = (per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
-  const bool dbl = p.dbl != 0;
+  // float-float moment products (FP64 only, one moment set)
+  constexpr bool FFM = K == kWsFF && !std::is_same<T, float>::value && VPT == 1;
+  const bool dbl = K == kWsMom && p.dbl != 0;
   const bool mom = p.vl != nullptr || dbl;
   // series step: series += c_m T_{m+1} (rec_A_vec), the accumulator tile staged like v_l
   constexpr bool ser = SER;
@@ -150,7 +161,6 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   int pending = 0;
   bool dead = false;
   // FP64 recursion, float-float moment products
-  const bool vlff = !F32 && VPT == 1 && p.vl_ff != 0 && !dbl;
   const double2* __restrict__ vl64 = static_cast<const double2*>(p.vl64);
   FFMom fm{0.f, 0.f, 0.f, 0.f};
   int ffp = 0;
@@ -164,7 +174,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
     }
   };
   auto flush_sets = [&](double2* dst) {
-    if (vlff) {
+    if constexpr (FFM) {
       ff_fold(mr[0], mi[0], fm);
       ffp = 0;
     }
@@ -253,7 +263,23 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
           continue;
         }
         if (!mom) continue;
-        if (dbl) {
+        if constexpr (FFM) {
+          const FF lf = ff_from_slot(l[u].re[0], l[u].im[0]);
+          FF tf;
+          bool ok = ff_split_f64(acc[u].re[0], tf.rh, tf.rl);
+          ok &= ff_split_f64(acc[u].im[0], tf.ih, tf.il);
+          ok &= ff_left_ok(lf.rh) & ff_left_ok(lf.ih);
+          if (ok) {
+            ff_cdot(fm, lf, tf);
+          } else {
+            const double2 lv = __ldg(vl64 + vi);
+            cdot_acc(mr[0], mi[0], lv.x, lv.y, acc[u].re[0], acc[u].im[0]);
+          }
+          if (++ffp == kFfFoldRows) {
+            ffp = 0;
+            ff_fold(mr[0], mi[0], fm);
+          }
+        } else if (dbl) {
           Cx<T, VPT> own;  // T_m at this row
           unpack(__ldg(tcur + vi), own);
 #pragma unroll
@@ -264,24 +290,6 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
             } else {
               cdot_acc(mr[q], mi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
               mr2[q] += fma(own.re[q], own.re[q], fma(own.im[q], own.im[q], -hvs[u][q]));
-            }
-          }
-        } else if (vlff) {
-          if constexpr (!F32) {
-            const FF lf = ff_from_slot(l[u].re[0], l[u].im[0]);
-            FF tf;
-            bool ok = ff_split_f64(acc[u].re[0], tf.rh, tf.rl);
-            ok &= ff_split_f64(acc[u].im[0], tf.ih, tf.il);
-            ok &= ff_left_ok(lf.rh) & ff_left_ok(lf.ih);
-            if (ok) {
-              ff_cdot(fm, lf, tf);
-            } else {
-              const double2 lv = __ldg(vl64 + vi);
-              cdot_acc(mr[0], mi[0], lv.x, lv.y, acc[u].re[0], acc[u].im[0]);
-            }
-            if (++ffp == kFfFoldRows) {
-              ffp = 0;
-              ff_fold(mr[0], mi[0], fm);
             }
           }
         } else {
@@ -319,11 +327,11 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   }
 }
 
-template <typename T, bool REAL, int TPR, int VPT, int U, bool SER>
+template <typename T, bool REAL, int TPR, int VPT, int U, int K>
 bool ws_smem_attr(size_t smem) {
   static size_t configured = 0;
   if (smem <= configured) return true;
-  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, SER>,
+  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -337,12 +345,22 @@ bool ws_smem_attr(size_t smem) {
 template <typename T, bool REAL, int TPR, int VPT, int U>
 int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
+  bool launched = false;
   if (p.series && !p.vl && !p.dbl) {
-    if (!ws_smem_attr<T, REAL, TPR, VPT, U, true>(smem)) return KPM_ERR_UNSUPPORTED;
-    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, true><<<grid, kWsThreads, smem, s>>>(p);
-  } else {
-    if (!ws_smem_attr<T, REAL, TPR, VPT, U, false>(smem)) return KPM_ERR_UNSUPPORTED;
-    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, false><<<grid, kWsThreads, smem, s>>>(p);
+    if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsSeries>(smem)) return KPM_ERR_UNSUPPORTED;
+    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsSeries><<<grid, kWsThreads, smem, s>>>(p);
+    launched = true;
+  }
+  if constexpr (sizeof(T) == 8 && VPT == 1) {
+    if (!launched && p.vl_ff && p.vl && !p.dbl) {
+      if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsFF>(smem)) return KPM_ERR_UNSUPPORTED;
+      cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsFF><<<grid, kWsThreads, smem, s>>>(p);
+      launched = true;
+    }
+  }
+  if (!launched) {
+    if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsMom>(smem)) return KPM_ERR_UNSUPPORTED;
+    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsMom><<<grid, kWsThreads, smem, s>>>(p);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -352,13 +370,14 @@ int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   return KPM_OK;
 }
 
+// CTAs of one SM (every epilogue variant has the same register bound)
 template <typename T, bool REAL, int TPR, int VPT, int U>
 int ws_ctas_per_sm(int L, int nvec) {
   const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
   if (smem > 200 * 1024) return 0;
-  if (!ws_smem_attr<T, REAL, TPR, VPT, U, false>(smem)) return 0;
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsMom>(smem)) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, false>, kWsThreads,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsMom>, kWsThreads,
                                                     smem) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;

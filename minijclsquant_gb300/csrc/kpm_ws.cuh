@@ -46,9 +46,10 @@ constexpr int kWsThreads = kBlock + 32;  // compute warps + one producer warp
 
 // Epilogue variants (template parameter K): each instantiation carries only its own code, so
 // the registers of one do not limit the occupancy of another.
-constexpr int kWsMom = 0;     // FP64 / complex64 moments (one set or doubled), or store only
+constexpr int kWsMom = 0;     // FP64 / complex64 moments (one set), or store only
 constexpr int kWsSeries = 1;  // series step
 constexpr int kWsFF = 2;      // FP64 recursion, one moment set with float-float products
+constexpr int kWsDbl = 3;     // doubled moments (two sets per step)
 
 template <typename T, bool REAL, int TPR, int VPT, int U, int K>
 __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && TPR >= 2) ? 3 : 2) : 1))
@@ -60,6 +61,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   constexpr int TILE = RPB * U;
   constexpr bool F32 = std::is_same<T, float>::value;
   constexpr bool SER = K == kWsSeries;
+  constexpr bool DBL = K == kWsDbl;
   constexpr int kFlush = 8;
   constexpr int kWarps = kBlock / 32;
 
@@ -112,8 +114,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       tc.col_slab = TILE * 4;
       tc.val_slab = (uint32_t)(TILE * sizeof(MV));
       tc.vec_slab = vec_b;
-      tc.vl_slab = p.dbl ? (uint32_t)(TILE * R * sizeof(T)) : vec_b;
-      if (p.dbl) tc.vl = static_cast<const unsigned char*>(p.hv);
+      tc.vl_slab = DBL ? (uint32_t)(TILE * R * sizeof(T)) : vec_b;
+      if (DBL) tc.vl = static_cast<const unsigned char*>(p.hv);
       tc.col_b = col_b;
       tc.val_b = val_b;
       tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + vec_b + (tc.vl ? tc.vl_slab : 0);
@@ -139,7 +141,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   int cur_inst = (per_tile && my_count > 0) ? p.tile_inst[seg_tb] : 0;
   // float-float moment products (FP64 only, one moment set)
   constexpr bool FFM = K == kWsFF && !std::is_same<T, float>::value && VPT == 1;
-  const bool dbl = K == kWsMom && p.dbl != 0;
+  constexpr bool dbl = DBL;
   const bool mom = p.vl != nullptr || dbl;
   // series step: series += c_m T_{m+1} (rec_A_vec), the accumulator tile staged like v_l
   constexpr bool ser = SER;
@@ -346,7 +348,11 @@ template <typename T, bool REAL, int TPR, int VPT, int U>
 int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
   bool launched = false;
-  if (p.series && !p.vl && !p.dbl) {
+  if (p.dbl) {
+    if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsDbl>(smem)) return KPM_ERR_UNSUPPORTED;
+    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsDbl><<<grid, kWsThreads, smem, s>>>(p);
+    launched = true;
+  } else if (p.series && !p.vl) {
     if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsSeries>(smem)) return KPM_ERR_UNSUPPORTED;
     cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsSeries><<<grid, kWsThreads, smem, s>>>(p);
     launched = true;

@@ -443,9 +443,10 @@ __global__ void __launch_bounds__(kBlock) cheb_step_kernel(const StepParams p) {
         unpack(ser[vi], o);
 #pragma unroll
         for (int k = 0; k < VPT; ++k) {
-          // axpy2(c_m, 1, T1, A_kpm): y = c_m*x + 1*y
-          o.re[k] = ((T)c_hi.x * acc.re[k] - (T)c_hi.y * acc.im[k]) + o.re[k];
-          o.im[k] = ((T)c_hi.x * acc.im[k] + (T)c_hi.y * acc.re[k]) + o.im[k];
+          // axpy2(c_m, 1, T1, A_kpm): y = c_m*x + 1*y as two nested FMAs per component (the
+          // producer-warp series step uses the same expression)
+          o.re[k] = fma((T)c_hi.x, acc.re[k], fma(-(T)c_hi.y, acc.im[k], o.re[k]));
+          o.im[k] = fma((T)c_hi.x, acc.im[k], fma((T)c_hi.y, acc.re[k], o.im[k]));
         }
       }
       ser[vi] = pack(o);

@@ -257,9 +257,9 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
           Cx<T, VPT> o;
 #pragma unroll
           for (int q = 0; q < VPT; ++q) {
-            // y = c_m*x + 1*y, the expression of the grid-stride kernel
-            o.re[q] = ((T)cm.x * acc[u].re[q] - (T)cm.y * acc[u].im[q]) + l[u].re[q];
-            o.im[q] = ((T)cm.x * acc[u].im[q] + (T)cm.y * acc[u].re[q]) + l[u].im[q];
+            // y = c_m*x + 1*y, the expression of the grid-stride kernel (two nested FMAs)
+            o.re[q] = fma((T)cm.x, acc[u].re[q], fma(-(T)cm.y, acc[u].im[q], l[u].re[q]));
+            o.im[q] = fma((T)cm.x, acc[u].im[q], fma((T)cm.y, acc[u].re[q], l[u].im[q]));
           }
           series[vi] = pack(o);
           continue;

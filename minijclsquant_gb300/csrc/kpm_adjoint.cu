@@ -538,7 +538,7 @@ int kpm_adjoint_forward(kpm_ell* h, int R, int M, int ckpt, const double* v, dou
   const size_t vb = (size_t)h->n_pad * R * sizeof(double2);
   const int nseg = (M - 1 + ckpt - 1) / ckpt;
   StepConfig cfg;
-  KPM_TRY(step_config(h, false, R, 1, s, &cfg));
+  KPM_TRY(step_config(h, false, R, kSetsFp64Products, s, &cfg));  // FP64 moments: the checkpointed forward
   KPM_TRY(ensure(ws.ta, vb));
   KPM_TRY(ensure(ws.tb, vb));
   KPM_TRY(ensure(ws.vl, vb));

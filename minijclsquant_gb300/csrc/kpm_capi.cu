@@ -181,7 +181,8 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
       if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
       const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2)
                                        : staged_ctas_f64(h->is_real, Rg, U, h->L, 2))
-                                : (f32 ? ws_ctas_f32(h->is_real, Rg, U, h->L, 2) : ws_ctas_f64(h->is_real, Rg, U, h->L, 2));
+                                : (f32 ? ws_ctas_f32(h->is_real, Rg, U, h->L, 2)
+                                       : ws_ctas_f64(h->is_real, Rg, U, h->L, 2, ffm));
       if (occ <= 0) continue;
       const int64_t ntiles = h->n_pad / staged_tile_rows(f32, Rg, U);
       StepConfig c;

@@ -35,8 +35,8 @@ int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaSt
   return Ws<double>::launch(real, R, U, p, grid, s);
 }
 
-int ws_ctas_f64(bool real, int R, int U, int L, int nvec) {
-  return Ws<double>::ctas_per_sm(real, R, U, L, nvec);
+int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff) {
+  return Ws<double>::ctas_per_sm(real, R, U, L, nvec, ff);
 }
 
 }  // namespace kpm

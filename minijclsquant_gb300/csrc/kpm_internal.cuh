@@ -172,7 +172,8 @@ int staged_ctas_f32(bool real, int R, int U, int L, int nvec);
 // The same step with a producer warp and full/empty stage barriers (kpm_ws.cuh).
 int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
 int launch_ws_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
-int ws_ctas_f64(bool real, int R, int U, int L, int nvec);
+// ff: CTAs of the float-float-products variant (one moment set, FP64 recursion)
+int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff = false);
 int ws_ctas_f32(bool real, int R, int U, int L, int nvec);
 // Driver helpers (kpm_capi.cu).
 int pow2_group(int remaining);
@@ -238,6 +239,10 @@ int pack_left_ff(const double* v, int64_t n, int64_t n_pad, int R, int r0, int R
 // FP64 one-set moments form their products in float-float arithmetic (producer-warp
 // kernel) unless KPM_MOMENTS_FP64 is set to a nonzero value.
 bool ff_moment_products(bool f32, int sets);
+// step_config moment-set codes: 1 one set, 2 two sets, 3 doubled, 4 series, and
+// kSetsFp64Products: one set whose products stay FP64 (callers that launch the FP64
+// moment variant themselves)
+constexpr int kSetsFp64Products = 5;
 int ensure_f32_values(kpm_ell_s* h, cudaStream_t s);
 // Profiling helpers: bracket a step loop with events when h->prof is set.
 int prof_begin(kpm_ell_s* h, cudaStream_t s, cudaEvent_t* ev);

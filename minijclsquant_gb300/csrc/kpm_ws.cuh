@@ -51,8 +51,15 @@ constexpr int kWsSeries = 1;  // series step
 constexpr int kWsFF = 2;      // FP64 recursion, one moment set with float-float products
 constexpr int kWsDbl = 3;     // doubled moments (two sets per step)
 
+// Shared-memory stages of one instantiation: three for the one-vector float-float step of a
+// real operator (three of its 20 KB stages per CTA let three CTAs share an SM), four otherwise.
+template <typename T, bool REAL, int TPR, int U, int K>
+__host__ __device__ constexpr int ws_stages() {
+  return (sizeof(T) == 8 && REAL && TPR == 1 && U == 1 && K == kWsFF) ? 3 : kWsStages;
+}
+
 template <typename T, bool REAL, int TPR, int VPT, int U, int K>
-__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && TPR >= 2) ? 3 : 2) : 1))
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : 1))
     cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;
@@ -62,12 +69,13 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   constexpr bool F32 = std::is_same<T, float>::value;
   constexpr bool SER = K == kWsSeries;
   constexpr bool DBL = K == kWsDbl;
+  constexpr int NST = ws_stages<T, REAL, TPR, U, K>();
   constexpr int kFlush = 8;
   constexpr int kWarps = kBlock / 32;
 
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full[kWsStages];
-  __shared__ __align__(8) uint64_t empty[kWsStages];
+  __shared__ __align__(8) uint64_t full[NST];
+  __shared__ __align__(8) uint64_t empty[NST];
   __shared__ double2 red[kWarps * R];
 
   const int L = p.L;
@@ -90,7 +98,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
 
   if (threadIdx.x == 0) {
 #pragma unroll
-    for (int s = 0; s < kWsStages; ++s) {
+    for (int s = 0; s < NST; ++s) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kWarps);
     }
@@ -121,8 +129,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + vec_b + (tc.vl ? tc.vl_slab : 0);
       int issued = 0;
       for (int k = 0; k < my_count; ++k) {
-        const int st = k % kWsStages;
-        if (k >= kWsStages && !mbar_wait_bounded(&empty[st], (uint32_t)(((k / kWsStages) - 1) & 1))) {
+        const int st = k % NST;
+        if (k >= NST && !mbar_wait_bounded(&empty[st], (uint32_t)(((k / NST) - 1) & 1))) {
           atomicExch(p.err, KPM_ERR_TIMEOUT);
           break;
         }
@@ -131,8 +139,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
         issued = k + 1;
       }
       // copies of the last stages may still be landing: wait for them before leaving
-      for (int q = issued > kWsStages ? issued - kWsStages : 0; q < issued; ++q)
-        (void)mbar_wait_bounded(&full[q % kWsStages], (uint32_t)((q / kWsStages) & 1));
+      for (int q = issued > NST ? issued - NST : 0; q < issued; ++q)
+        (void)mbar_wait_bounded(&full[q % NST], (uint32_t)((q / NST) & 1));
     }
     return;
   }
@@ -187,8 +195,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   };
 
   for (int k = 0; k < my_count; ++k) {
-    const int st = k % kWsStages;
-    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / kWsStages) & 1));
+    const int st = k % NST;
+    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / NST) & 1));
     ok = __all_sync(0xffffffffu, ok);
     if (!ok && !dead) {
       if (lane == 0) atomicExch(p.err, KPM_ERR_TIMEOUT);
@@ -346,7 +354,8 @@ bool ws_smem_attr(size_t smem) {
 
 template <typename T, bool REAL, int TPR, int VPT, int U>
 int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
-  const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
+  const size_t stage = staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
+  const size_t smem = kWsStages * stage;
   bool launched = false;
   if (p.dbl) {
     if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsDbl>(smem)) return KPM_ERR_UNSUPPORTED;
@@ -359,8 +368,9 @@ int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   }
   if constexpr (sizeof(T) == 8 && VPT == 1) {
     if (!launched && p.vl_ff && p.vl && !p.dbl) {
-      if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsFF>(smem)) return KPM_ERR_UNSUPPORTED;
-      cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsFF><<<grid, kWsThreads, smem, s>>>(p);
+      const size_t smem_ff = ws_stages<T, REAL, TPR, U, kWsFF>() * stage;
+      if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsFF>(smem_ff)) return KPM_ERR_UNSUPPORTED;
+      cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsFF><<<grid, kWsThreads, smem_ff, s>>>(p);
       launched = true;
     }
   }
@@ -376,19 +386,30 @@ int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   return KPM_OK;
 }
 
-// CTAs of one SM (every epilogue variant has the same register bound)
-template <typename T, bool REAL, int TPR, int VPT, int U>
-int ws_ctas_per_sm(int L, int nvec) {
-  const size_t smem = kWsStages * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
+// CTAs of one SM for epilogue variant K
+template <typename T, bool REAL, int TPR, int VPT, int U, int K>
+int ws_ctas_per_sm_k(int L, int nvec) {
+  const size_t smem = ws_stages<T, REAL, TPR, U, K>() * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
   if (smem > 200 * 1024) return 0;
-  if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsMom>(smem)) return 0;
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U, K>(smem)) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsMom>, kWsThreads,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K>, kWsThreads,
                                                     smem) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;
   }
   return n;
+}
+
+// ff: the launches will be the float-float-products variant (its stage count and register
+// bound can differ); otherwise the moment variant, whose bound the series and doubled
+// variants share
+template <typename T, bool REAL, int TPR, int VPT, int U>
+int ws_ctas_per_sm(int L, int nvec, bool ff) {
+  if constexpr (sizeof(T) == 8 && VPT == 1) {
+    if (ff) return ws_ctas_per_sm_k<T, REAL, TPR, VPT, U, kWsFF>(L, nvec);
+  }
+  return ws_ctas_per_sm_k<T, REAL, TPR, VPT, U, kWsMom>(L, nvec);
 }
 
 // Dispatch over (real, R, U) for one precision (VPT as in the staged kernel).
@@ -400,17 +421,17 @@ struct Ws {
     return launch_ws<T, REAL, R / VPT, VPT, U>(p, grid, s);
   }
   template <bool REAL, int R, int U>
-  static int occ(int L, int nvec) {
+  static int occ(int L, int nvec, bool ff) {
     constexpr int VPT = (std::is_same<T, float>::value && R >= 2) ? 2 : 1;
-    return ws_ctas_per_sm<T, REAL, R / VPT, VPT, U>(L, nvec);
+    return ws_ctas_per_sm<T, REAL, R / VPT, VPT, U>(L, nvec, ff);
   }
   template <bool REAL, int R>
   static int go_u(int U, const StepParams& p, int grid, cudaStream_t s) {
     return U == 2 ? go<REAL, R, 2>(p, grid, s) : go<REAL, R, 1>(p, grid, s);
   }
   template <bool REAL, int R>
-  static int occ_u(int U, int L, int nvec) {
-    return U == 2 ? occ<REAL, R, 2>(L, nvec) : occ<REAL, R, 1>(L, nvec);
+  static int occ_u(int U, int L, int nvec, bool ff) {
+    return U == 2 ? occ<REAL, R, 2>(L, nvec, ff) : occ<REAL, R, 1>(L, nvec, ff);
   }
   template <bool REAL>
   static int go_r(int R, int U, const StepParams& p, int grid, cudaStream_t s) {
@@ -423,20 +444,20 @@ struct Ws {
     }
   }
   template <bool REAL>
-  static int occ_r(int R, int U, int L, int nvec) {
+  static int occ_r(int R, int U, int L, int nvec, bool ff) {
     switch (R) {
-      case 1: return occ_u<REAL, 1>(U, L, nvec);
-      case 2: return occ_u<REAL, 2>(U, L, nvec);
-      case 4: return occ_u<REAL, 4>(U, L, nvec);
-      case 8: return occ_u<REAL, 8>(U, L, nvec);
+      case 1: return occ_u<REAL, 1>(U, L, nvec, ff);
+      case 2: return occ_u<REAL, 2>(U, L, nvec, ff);
+      case 4: return occ_u<REAL, 4>(U, L, nvec, ff);
+      case 8: return occ_u<REAL, 8>(U, L, nvec, ff);
       default: return 0;
     }
   }
   static int launch(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
     return real ? go_r<true>(R, U, p, grid, s) : go_r<false>(R, U, p, grid, s);
   }
-  static int ctas_per_sm(bool real, int R, int U, int L, int nvec) {
-    return real ? occ_r<true>(R, U, L, nvec) : occ_r<false>(R, U, L, nvec);
+  static int ctas_per_sm(bool real, int R, int U, int L, int nvec, bool ff = false) {
+    return real ? occ_r<true>(R, U, L, nvec, ff) : occ_r<false>(R, U, L, nvec, ff);
   }
 };
 

@@ -3,25 +3,26 @@
 //   T_{m+1} = 2H T_m - T_{m-1}  (in place over T_{m-1})  and  <v_l | T_{m+1}>
 //
 // Same tile layout and per-tile bulk copies as the staged kernel, but the CTA is
-// split into kBlock compute threads and one producer warp.  Each of the
-// kWsStages shared-memory stages has a "full" mbarrier (the producer's
-// expect_tx, completed by the copies) and an "empty" mbarrier (one arrival per
-// compute warp once it has read the stage).  Compute warps never meet at a
+// split into kBlock compute threads and one producer warp.  Each of the NST
+// shared-memory stages (ws_stages: four, or three for the one-vector float-float
+// step) has a "full" mbarrier (the producer's expect_tx, completed by the copies)
+// and an "empty" mbarrier (one arrival per compute warp once it has read the stage).  Compute warps never meet at a
 // CTA-wide barrier inside the tile loop, so while one warp waits on its
 // neighbour gathers T_m[col] the others compute, and the producer refills a
 // stage as soon as the last warp has left it.
 //
-// The series instantiation (K = kWsSeries) is a series step of rec_A_vec (p.series set, p.vl null, no
-// doubling): the producer stages the series accumulator tile in the left-vector
-// slot and the compute warps write back series + c_m T_{m+1}; no moments are formed.
+// The series instantiation (K = kWsSeries) is a series step of rec_A_vec (p.series
+// set, p.vl null, no doubling): the producer stages the series accumulator tile in
+// the left-vector slot and the compute warps write back series + c_m T_{m+1}; no
+// moments are formed.
 //
 // Moment partials follow the staged kernel: per CTA (strided tiles) or, for
 // batched operators (per_tile), flushed per (CTA, instance) run with a block
 // reduction over the compute warps alone (named barrier 1).  With p.vl null the
 // step stores T_{m+1} only (no left vector is copied, no moments), and with
 // p.tprev set T_{m-1} is read from there (out of place) instead of from tout.
-// With p.dbl (doubling) the producer stages |v|^2 / 2 in place of the left
-// vector and the two moment sets <T_{m+1}|T_m>, sum (|T_m|^2 - |v|^2 / 2) are
+// With p.dbl (doubling; K = kWsDbl) the producer stages |v|^2 / 2 in place of the
+// left vector and the two moment sets <T_{m+1}|T_m>, sum (|T_m|^2 - |v|^2 / 2) are
 // accumulated (T_m's own row read from tcur).
 //
 // With p.vl_ff (FP64 only, one moment set; K = kWsFF) the staged left vector holds float

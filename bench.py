@@ -497,7 +497,7 @@ def run_driven(a, hbm_peak):
            "mu0_over_n": float(abs(mu[0].item()) / g.n),
            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
                         "kernel": "light_update_kernel", "algorithmic_bytes_per_update": slots * 64,
-                        "limiter": "FP64 pipe: one sincos per slot with a nonzero phase (the bond slots)"},
+                        "limiter": "FP64 pipe: per bond slot one table-driven sin/cos and two complex products"},
            "note": "kpm_ell_light_update: H(t) into the operator's stored values, once per time step"}
     del op, g
     torch.cuda.empty_cache()

@@ -14,12 +14,15 @@
 // The time-dependent scalars (cos wt, sin wt, the pulse envelope) are evaluated once on
 // the host in complex double arithmetic, as the reference evaluates them per element;
 // per element the kernels do complex multiplies and one complex exponential
-// exp(x + iy) = e^x (cos y + i sin y).  Streaming kernels, HBM-bound, run once per time
-// step (recomputing the phases inside every recursion step would add a sincos per slot
-// per step to an FP64-bound kernel).
+// exp(x + iy) = e^x (cos y + i sin y).  The light kernels take sin y and cos y from a
+// 256-entry table and short polynomials (sincos_tab): the FP64 pipe, 1/64 of the FP32
+// rate on GB300, bounds these kernels, and the table form needs fewer FP64 instructions.
+// They run once per time step (recomputing the phases inside every recursion step would
+// add that work per slot per step to an FP64-bound kernel).
 #include <algorithm>
 #include <cmath>
 #include <complex>
+#include <mutex>
 
 #include "kpm_internal.cuh"
 
@@ -44,6 +47,83 @@ __device__ __forceinline__ double2 cexp2(double2 z) {
   const double e = z.x == 0.0 ? 1.0 : exp(z.x);  // a pure phase (real pulse parameters): exp(0) = 1
   return make_double2(e * c, e * s);
 }
+// sin x and cos x by table lookup: P. T. P. Tang, "Table-lookup algorithms for elementary
+// functions and their error analysis" (1991), with the three-part argument reduction of
+// W. J. Cody and W. Waite, "Software Manual for the Elementary Functions" (1980).
+// x = k 2pi/256 + r with |r| <= pi/256 (2pi/256 split into parts of 32, 32 and 53
+// significant bits, so k C1 and k C2 are exact for |k| < 2^21); then
+//   sin x = S_k cos r + C_k sin r,   cos x = C_k cos r - S_k sin r,
+// with (S_k, C_k) = (sin, cos)(2pi k / 256) from the table and the Taylor series of sin r
+// to r^7 and of cos r to r^6 (the next terms are below 2e-20).  Absolute error below
+// 2e-16.  |x| > 2e4, and NaN, go to sincos().
+constexpr double kScC1 = 0x1.921fb54400000p-6;
+constexpr double kScC2 = 0x1.0b4611a600000p-40;
+constexpr double kScC3 = 0x1.3198a2e037073p-75;
+constexpr double kScInv = 40.74366543152521;  // 256 / (2 pi)
+
+__device__ __forceinline__ void sincos_tab(double x, const double2* __restrict__ tab, double* s, double* c) {
+  if (!(fabs(x) <= 2.0e4)) {
+    sincos(x, s, c);
+    return;
+  }
+  const double kd = rint(x * kScInv);
+  double r = fma(-kd, kScC1, x);
+  r = fma(-kd, kScC2, r);
+  r = fma(-kd, kScC3, r);
+  const double2 t = __ldg(tab + ((int)kd & 255));  // (S_k, C_k); k mod 256 in two's complement
+  const double r2 = r * r;
+  const double sr = fma(r * r2, fma(r2, fma(r2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), r);
+  const double cr = fma(r2, fma(r2, fma(r2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
+  *s = fma(t.x, cr, t.y * sr);
+  *c = fma(t.y, cr, -(t.x * sr));
+}
+__device__ __forceinline__ double2 cexp_tab(double2 z, const double2* __restrict__ tab) {
+  double s, c;
+  sincos_tab(z.y, tab, &s, &c);
+  if (z.x == 0.0) return make_double2(c, s);  // a pure phase (real pulse parameters)
+  const double e = exp(z.x);
+  return make_double2(e * c, e * s);
+}
+// kx dx + ky dy; with real bond vectors (their usual form) two FMAs per component
+__device__ __forceinline__ double2 light_arg(double2 kx, double2 ky, double2 dx, double2 dy) {
+  if (dx.y == 0.0 && dy.y == 0.0)
+    return make_double2(fma(kx.x, dx.x, ky.x * dy.x), fma(kx.y, dx.x, ky.y * dy.x));
+  return cadd(cmul(kx, dx), cmul(ky, dy));
+}
+
+// The (sin, cos)(2pi k / 256) table of the current device, made once on the host in long
+// double and rounded to double.
+const double2* sincos_table(int* status) {
+  static std::mutex mu;
+  static double2* tab[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64) {
+    *status = e != cudaSuccess ? check_cuda(e) : KPM_ERR_UNSUPPORTED;
+    return nullptr;
+  }
+  std::lock_guard<std::mutex> lock(mu);
+  if (!tab[dev]) {
+    double2 host[256];
+    const long double two_pi = 6.283185307179586476925286766559005768L;
+    for (int k = 0; k < 256; ++k) {
+      const long double a = two_pi * (long double)k / 256.0L;
+      host[k] = make_double2((double)sinl(a), (double)cosl(a));
+    }
+    double2* d = nullptr;
+    e = cudaMalloc(&d, sizeof(host));
+    if (e == cudaSuccess) e = cudaMemcpy(d, host, sizeof(host), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      if (d) cudaFree(d);
+      *status = check_cuda(e);
+      return nullptr;
+    }
+    tab[dev] = d;
+  }
+  *status = KPM_OK;
+  return tab[dev];
+}
+
 // cos(x + iy) = cos x cosh y - i sin x sinh y
 __device__ __forceinline__ double2 ccos2(double2 z) {
   double s, c;
@@ -76,10 +156,11 @@ void light_coefficients(const double* params, double2* a, double2* kx, double2* 
 }
 
 __global__ void light_kernel(int64_t count, double2 a, double2 kx, double2 ky, const double2* __restrict__ data,
-                             const double2* __restrict__ dx, const double2* __restrict__ dy, double2* __restrict__ out) {
+                             const double2* __restrict__ dx, const double2* __restrict__ dy, double2* __restrict__ out,
+                             const double2* __restrict__ tab) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
-    const double2 z = cadd(cmul(kx, dx[i]), cmul(ky, dy[i]));
-    out[i] = cmul(cmul(a, data[i]), cexp2(z));
+    const double2 z = light_arg(kx, ky, dx[i], dy[i]);
+    out[i] = cmul(cmul(a, data[i]), cexp_tab(z, tab));
   }
 }
 
@@ -89,16 +170,17 @@ __global__ void light_kernel(int64_t count, double2 a, double2 kx, double2 ky, c
 // exactly.  Stores are whole 128-byte segments of each slot plane s * n_pad + row; the
 // row's L consecutive inputs come through L1.  Padding rows (row >= n) keep the zeros
 // written at creation.
-__global__ void light_update_kernel(int64_t n, int64_t n_pad, int L, double2 a, double2 kx, double2 ky,
+// a2 = 2a: the stored values are 2H (doubling is exact, so 2a data e = 2 (a data e) bit for bit).
+__global__ void light_update_kernel(int64_t n, int64_t n_pad, int L, double2 a2, double2 kx, double2 ky,
                                     const double2* __restrict__ data, const double2* __restrict__ dx,
-                                    const double2* __restrict__ dy, double2* __restrict__ val) {
+                                    const double2* __restrict__ dy, double2* __restrict__ val,
+                                    const double2* __restrict__ tab) {
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
     for (int s = 0; s < L; ++s) {
       const int64_t k = row * L + s;
-      const double2 z = cadd(cmul(kx, dx[k]), cmul(ky, dy[k]));
-      const double2 e = (z.x == 0.0 && z.y == 0.0) ? make_double2(1.0, 0.0) : cexp2(z);
-      const double2 v = cmul(cmul(a, data[k]), e);
-      val[(int64_t)s * n_pad + row] = make_double2(2.0 * v.x, 2.0 * v.y);
+      const double2 z = light_arg(kx, ky, dx[k], dy[k]);
+      const double2 e = (z.x == 0.0 && z.y == 0.0) ? make_double2(1.0, 0.0) : cexp_tab(z, tab);
+      val[(int64_t)s * n_pad + row] = cmul(cmul(a2, data[k]), e);
     }
   }
 }
@@ -154,11 +236,14 @@ int kpm_light_modifier(int64_t count, const double* params, const double* data, 
   if (count < 1 || !params || !data || !dx || !dy || !data_new) return KPM_ERR_INVALID_ARG;
   double2 a, kx, ky;
   light_coefficients(params, &a, &kx, &ky);
+  int st = KPM_OK;
+  const double2* tab = sincos_table(&st);
+  if (!tab) return st;
   cudaStream_t s = stream_of(stream);
   light_kernel<<<grid_for_count(count), 256, 0, s>>>(count, a, kx, ky, reinterpret_cast<const double2*>(data),
                                                      reinterpret_cast<const double2*>(dx),
                                                      reinterpret_cast<const double2*>(dy),
-                                                     reinterpret_cast<double2*>(data_new));
+                                                     reinterpret_cast<double2*>(data_new), tab);
   return check_cuda(cudaGetLastError());
 }
 
@@ -168,10 +253,13 @@ int kpm_ell_light_update(kpm_ell* h, const double* params, const double* data0, 
   if (h->is_real) return KPM_ERR_DTYPE;  // H(t) is complex: create the operator with KPM_FLAG_COMPLEX
   double2 a, kx, ky;
   light_coefficients(params, &a, &kx, &ky);
+  int st = KPM_OK;
+  const double2* tab = sincos_table(&st);
+  if (!tab) return st;
   cudaStream_t s = stream_of(stream);
   light_update_kernel<<<grid_for_count(h->n), 256, 0, s>>>(
-      h->n, h->n_pad, h->L, a, kx, ky, reinterpret_cast<const double2*>(data0), reinterpret_cast<const double2*>(dx),
-      reinterpret_cast<const double2*>(dy), static_cast<double2*>(h->val64));
+      h->n, h->n_pad, h->L, make_double2(2.0 * a.x, 2.0 * a.y), kx, ky, reinterpret_cast<const double2*>(data0), reinterpret_cast<const double2*>(dx),
+      reinterpret_cast<const double2*>(dy), static_cast<double2*>(h->val64), tab);
   KPM_TRY(check_cuda(cudaGetLastError()));
   return values_changed(h, s);
 }

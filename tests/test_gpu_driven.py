@@ -183,3 +183,29 @@ def test_phonon_modifier_rejects_columns_outside_the_operator(cuda_lib):
     assert _capi.lib().kpm_light_modifier(0, p.ctypes.data, d.data_ptr(), x.data_ptr(), y.data_ptr(), dn.data_ptr(),
                                           None) == _capi.KPM_ERR_INVALID_ARG
     assert isinstance(ctypes.c_int(st).value, int)
+
+
+def test_light_phase_table_accuracy(cuda_lib):
+    """The light kernels' table-driven sin and cos (256-entry table, Cody-Waite reduction,
+    Taylor polynomials): exp(i x) for data = 1 and the circular form at t = 0 (arg = i A0 dx),
+    within 4e-16 absolute of numpy's cos and sin, on small, O(1), near-multiple-of-pi/2 and
+    large arguments, and above 2e4 where the kernels fall back to sincos()."""
+    import torch
+
+    rng = np.random.default_rng(3)
+    k = rng.integers(-5000, 5000, 20000)
+    x = np.concatenate([rng.uniform(-4, 4, 200000), rng.uniform(-2e4, 2e4, 200000),
+                        np.ldexp(rng.uniform(-1, 1, 20000), -rng.integers(1, 60, 20000)),
+                        k * (np.pi / 2) + rng.uniform(-1e-9, 1e-9, k.size), rng.uniform(2e4, 1e6, 5000),
+                        [0.0, -0.0, 2e4, -2e4, np.pi, -np.pi]])
+    n = x.size
+    d = torch.ones(n, dtype=torch.complex128, device="cuda")
+    dx = torch.from_numpy(x.astype(np.complex128)).cuda()
+    dy = torch.zeros(n, dtype=torch.complex128, device="cuda")
+    out = torch.empty_like(d)
+    p = _params([1, 1, 0, 1, 0, 1])  # a, A0, t, w, Tp, eta
+    assert cuda_lib.kpm_light_modifier(n, p.ctypes.data, d.data_ptr(), dx.data_ptr(), dy.data_ptr(), out.data_ptr(),
+                                       None) == 0
+    o = out.cpu().numpy()
+    assert np.max(np.abs(o.real - np.cos(x))) <= 4e-16
+    assert np.max(np.abs(o.imag - np.sin(x))) <= 4e-16

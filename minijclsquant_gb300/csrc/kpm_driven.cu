@@ -54,8 +54,8 @@ __device__ __forceinline__ double2 cexp2(double2 z) {
 // significant bits, so k C1 and k C2 are exact for |k| < 2^21); then
 //   sin x = S_k cos r + C_k sin r,   cos x = C_k cos r - S_k sin r,
 // with (S_k, C_k) = (sin, cos)(2pi k / 256) from the table and the Taylor series of sin r
-// to r^7 and of cos r to r^6 (the next terms are below 2e-20).  Absolute error below
-// 2e-16.  |x| > 2e4, and NaN, go to sincos().
+// to r^7 and of cos r to r^6 (the next terms are below 2e-20).  Absolute error about
+// 1.5e-16.  |x| > 2e4, and NaN, go to sincos().
 constexpr double kScC1 = 0x1.921fb54400000p-6;
 constexpr double kScC2 = 0x1.0b4611a600000p-40;
 constexpr double kScC3 = 0x1.3198a2e037073p-75;

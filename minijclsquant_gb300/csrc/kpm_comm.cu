@@ -78,14 +78,12 @@ __global__ void __launch_bounds__(kBlock) comm_step_kernel(const CommParams p) {
     p.tout[vi] = pack(t);
     p.cout[vi] = pack(c);
     double2 a;
-    const double yr = cm.x * c.re[0] - cm.y * c.im[0];
-    const double yi = cm.x * c.im[0] + cm.y * c.re[0];
     if (FIRST) {
-      a = make_double2(yr, yi);
-    } else {
+      a = make_double2(cm.x * c.re[0] - cm.y * c.im[0], cm.x * c.im[0] + cm.y * c.re[0]);
+    } else {  // acc += c_m C_m as two nested FMAs per component
       a = p.acc[vi];
-      a.x = yr + a.x;
-      a.y = yi + a.y;
+      a.x = fma(cm.x, c.re[0], fma(-cm.y, c.im[0], a.x));
+      a.y = fma(cm.x, c.im[0], fma(cm.y, c.re[0], a.y));
     }
     p.acc[vi] = a;
   }

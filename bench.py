@@ -78,6 +78,8 @@ def parse():
     ap.add_argument("--kubo-cells", type=int, default=1024)
     ap.add_argument("--kubo-Nm", type=int, default=256)
     ap.add_argument("--kubo-R", type=int, default=4)
+    ap.add_argument("--no-config1", action="store_true", help="skip the 8192-site DOS configuration")
+    ap.add_argument("--e2e-max-steps", type=int, default=6, help="host-pointer passes timed for e2e")
     return ap.parse_args()
 
 
@@ -184,8 +186,9 @@ def cpu_reference_kernels():
         return None
 
 
-def cpu_rec_A_tab(M, prob, v, threads):
-    """One CPU recursion of M moments; returns (seconds, kind)."""
+def cpu_rec_A_tab(M, prob, v, threads, want_moments=False):
+    """One CPU recursion of M moments; returns (seconds, kind), or (seconds, kind, moments)
+    with want_moments."""
     blas = cpu_reference_kernels()
     n, L = prob["n"], prob["L"]
     if blas is not None:
@@ -202,12 +205,46 @@ def cpu_rec_A_tab(M, prob, v, threads):
             blas.aAxby(2.0 + 0j, -1 + 0j, T1, T0, data, idx, L, n, threads)
             T0, T1 = T1, T0
             A_vec[m] = blas.vdot(1 + 0j, v, T1, n, threads)
-        return time.perf_counter() - t0, "reference"
+        dt = time.perf_counter() - t0
+        return (dt, "reference", A_vec) if want_moments else (dt, "reference")
     from oracle import oracle
 
     t0 = time.perf_counter()
-    oracle.rec_A_tab(M, prob["data_kpm"], prob["indices"], L, v, threads=threads)
-    return time.perf_counter() - t0, "port"
+    A_vec = oracle.rec_A_tab(M, prob["data_kpm"], prob["indices"], L, v, threads=threads)
+    dt = time.perf_counter() - t0
+    return (dt, "port", A_vec) if want_moments else (dt, "port")
+
+
+def cpu_model():
+    """The host CPU as lscpu names it (model name, or vendor and model for Arm cores)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                             timeout=10).stdout
+        kv = {}
+        for line in out.splitlines():
+            if ":" in line:
+                k, v = line.split(":", 1)
+                kv.setdefault(k.strip(), v.strip())
+        name = kv.get("Model name") or kv.get("BIOS Model name")
+        vendor = kv.get("Vendor ID", "")
+        if name:
+            return (vendor + " " + name).strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+def moment_parity(mu, ref, rel=1e-10, floor_frac=1e-6):
+    """Per-order parity against the reference's moments: max_m |mu_m - ref_m| /
+    max(|ref_m|, floor_frac |ref_0|), with the order where it is largest."""
+    mu, ref = np.asarray(mu), np.asarray(ref)
+    scale = np.maximum(np.abs(ref), floor_frac * np.abs(ref[0]))
+    r = np.abs(mu[: len(ref)] - ref) / scale
+    return {"orders": int(len(ref)), "max_rel": float(np.max(r)), "at_order": int(np.argmax(r)),
+            "max_abs_over_mu0": float(np.max(np.abs(mu[: len(ref)] - ref)) / abs(ref[0])), "tolerance": rel,
+            "pass": bool(np.max(r) <= rel)}
 
 
 def cpu_time_evolve(M2, prob, vs, threads):
@@ -511,16 +548,18 @@ def ctypes_stream(stream):
 
 
 def cpu_baseline(prob, target_s):
+    """The reference's rec_A_tab loop on the host cores for vector seed 1000 (the GPU's vector 0
+    on rank 0); returns (block, moments) so the caller can check parity on the same input."""
     threads = os.cpu_count() or 1
     v = random_vectors(prob["n"], 1, 1000)[0]
     dt, kind = cpu_rec_A_tab(4, prob, v, threads)  # calibration (also warms caches)
     per_step = max(dt / 3, 1e-6)
     M = int(min(512, max(8, target_s / per_step)))
-    dt, kind = cpu_rec_A_tab(M, prob, v, threads)
+    dt, kind, mu = cpu_rec_A_tab(M, prob, v, threads, want_moments=True)
     steps = prob["n"] * (M - 1)
-    return {"value": steps / dt, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": "rec_A_tab loop, 1 vector, M=%d on the full %d-site operator (%d site-steps in %.2f s)"
-                      % (M, prob["n"], steps, dt)}
+    return {"value": steps / dt, "unit": UNIT, "cores": threads, "kind": kind, "cpu_model": cpu_model(),
+            "sample": "rec_A_tab loop, 1 vector (seed 1000), M=%d on the full %d-site operator (%d site-steps in "
+                      "%.2f s)" % (M, prob["n"], steps, dt)}, mu
 
 
 # ---------------------------------------------------------------------------
@@ -587,8 +626,13 @@ def run_reference_arm(a):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
-            "config": {"workload": workload_desc(a, prob["n"]), "sites": prob["n"], "M": a.M, "R": a.R},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample},
+            "config": {"workload": "plain c128 KPM moments on the %d-site honeycomb operator of the GPU arm "
+                                   "(2048x2048 cells, W=%g eV, ELL width 4); sampled at M=%d moments and R=1 "
+                                   "vector per step (the GPU arm runs M=%d, R=%d; the unit, site-steps/s, is "
+                                   "per site, vector and order)" % (prob["n"], a.W, M, a.M, a.R),
+                       "sites": prob["n"], "M": M, "R": 1, "gpu_arm_M": a.M, "gpu_arm_R": a.R},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
+                             "cpu_model": cpu_model()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -921,6 +965,143 @@ def run_kubo(a, peaks, steps, warmup):
             "fp64_check": {"block": "n, m in %s, vector 0" % sel, "max_abs_err_over_max": err}}
 
 
+def run_fp64_products(a, op, v, M, R, n, bytes_per_launch, hbm_peak, fma_peak, rec_fma, world, mu_default):
+    """The headline recursion with every moment product in FP64 (KPM_MOMENTS_FP64=1, read by
+    the library at each call): value, roofline of its step kernel, FP64 FMA rate, and the
+    per-order difference from the default (float-float products).  Returns (block, moments)."""
+    import ctypes
+
+    import torch
+
+    from minijclsquant_gb300 import _capi, device
+
+    lib = _capi.lib()
+    stream = torch.cuda.current_stream()
+    os.environ["KPM_MOMENTS_FP64"] = "1"
+    try:
+        mu = device.cheb_moments(op, M, v, dtype="c128")  # tunes the FP64-products step once
+        torch.cuda.synchronize()
+        k = max(1, min(a.steps, 3))
+        lib.kpm_ell_profile(op.handle, 1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            mu = device.cheb_moments(op, M, v, dtype="c128")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        loop_ms, launches, rows = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+        _capi.check(lib.kpm_ell_profile_read(op.handle, ctypes.byref(loop_ms), ctypes.byref(launches),
+                                             ctypes.byref(rows)))
+        lib.kpm_ell_profile(op.handle, 0)
+        kind, rpt, grid, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _capi.check(lib.kpm_ell_step_config(op.handle, _capi.KPM_C128, R, ctypes.byref(kind), ctypes.byref(rpt),
+                                            ctypes.byref(grid), ctypes.byref(us)))
+    finally:
+        del os.environ["KPM_MOMENTS_FP64"]
+    ms = max_over_ranks(e0.elapsed_time(e1), world) / k
+    launch_s = loop_ms.value * 1e-3 / max(1, launches.value)
+    gbs = bytes_per_launch / launch_s / 1e9
+    fma = (rec_fma + 4) * float(n) * R / launch_s
+    mu_h = mu.cpu().numpy()
+    d = np.abs(mu_h - mu_default) / np.maximum(np.abs(mu_h), 1e-6 * np.abs(mu_h[:, :1]))
+    blk = {"value": float(n) * R * (M - 1) * world / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms, "steps": k,
+           "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
+                        "kernel": "%s (FP64 moment products, %d row(s)/thread)"
+                                  % ({0: "cheb_step_kernel", 1: "cheb_next_staged_kernel",
+                                      2: "cheb_next_ws_kernel"}.get(kind.value, "?"), rpt.value),
+                        "grid": grid.value, "avg_launch_ms": launch_s * 1e3},
+           "fp64": {"achieved_fma_per_s": fma, "peak_fma_per_s": fma_peak, "frac": fma / fma_peak,
+                    "fma_per_site_step": rec_fma + 4},
+           "default_vs_fp64_products": {"max_rel_per_order": float(d.max()),
+                                        "max_abs_over_mu0": float(np.max(np.abs(mu_h - mu_default))
+                                                                  / np.max(np.abs(mu_h[:, 0])))},
+           "note": "KPM_MOMENTS_FP64=1: the all-FP64 complex128 recursion and moment products (strict form)"}
+    return blk, mu_h
+
+
+def run_config1(a, world):
+    """The CPU-runnable DOS configuration: honeycomb 64 x 64 cells (8,192 sites), W = 0.5 eV
+    (seed 1234), Gershgorin bound x 1.01, M = 512, R = 4 vectors (seeds 1000..1003), DOS on 1024
+    energies.  L2-resident, so launch- and latency-bound: reported as recursion steps/s and
+    site-steps/s (moments on the device, CUDA events), the host DOS reconstruction time, and the
+    whole drop-in call (numpy vectors in, DOS out) beside the reference's CPU path in the same
+    run: its rec_A_tab loop over jclsquant's own aAxby/vdot for the four vectors and its DOS
+    loop (jclsquant/observables.py:49-52: one moments_delta and one dot per energy)."""
+    import torch
+
+    from minijclsquant_gb300 import device
+    from minijclsquant_gb300.kernel_and_moments import JacksonKernel, moments_delta
+    from minijclsquant_gb300.observables import dos_from_moments
+
+    prob = build_problem(64, 0.5)
+    n, L = prob["n"], prob["L"]
+    M, R, n_e = 512, 4, 1024
+    vs = random_vectors(n, R, 1000)
+    op = device.DeviceELL(prob["data_kpm"], prob["indices"], L)
+    v = torch.from_numpy(vs).cuda()
+    for _ in range(max(3, a.warmup)):
+        mu = device.cheb_moments(op, M, v)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    k = max(10, a.steps)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(k):
+        mu = device.cheb_moments(op, M, v)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world) / k
+    mu_h = mu.cpu().numpy()
+    t0 = time.perf_counter()
+    dos = dos_from_moments(mu_h, prob["bounds"], M, n_e)
+    dos_s = time.perf_counter() - t0
+    # the whole call as a user makes it: host vectors in, moments back, DOS on the host
+    t0 = time.perf_counter()
+    for _ in range(k):
+        dos_e2e = dos_from_moments(device.cheb_moments(op, M, vs), prob["bounds"], M, n_e)
+    e2e_s = (time.perf_counter() - t0) / k
+    blk = {"workload": "honeycomb 64x64 cells (%d sites), W=0.5 eV, Gershgorin x 1.01, M=%d, R=%d, DOS on %d "
+                       "energies" % (n, M, R, n_e),
+           "value": float(n) * R * (M - 1) / (ms * 1e-3), "unit": UNIT, "ms_per_recursion": ms,
+           "recursion_steps_per_s": (M - 1) / (ms * 1e-3), "dos_reconstruction_ms": dos_s * 1e3,
+           "e2e": {"ms_per_dos": e2e_s * 1e3, "value": float(n) * R * (M - 1) / e2e_s, "unit": UNIT,
+                   "path": "device.cheb_moments(numpy [R, N]) + dos_from_moments (host FP64)"},
+           "bound": "launch/latency (8192 sites x R=4 stay in L2)",
+           "same_dos_twice": bool(np.array_equal(dos, dos_e2e))}
+    if not a.no_cpu and world == 1:
+        blas = cpu_reference_kernels()
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        mus = [cpu_rec_A_tab(M, prob, vs[r], threads, want_moments=True)[2] for r in range(R)]
+        cpu_rec_s = time.perf_counter() - t0
+        kind = "reference" if blas is not None else "port"
+        mu_c = np.mean(np.stack(mus), axis=0)
+        # the reference's DOS loop: per energy, moments_delta(E~) * Jackson, then its blas dot
+        b = prob["bounds"]
+        a_ = 0.5 * (b[1] - b[0])
+        Ef = np.linspace(b[0] + 1e-3, b[1] - 1e-3, n_e)
+        kern = JacksonKernel(M).astype(np.complex128)
+        t0 = time.perf_counter()
+        rho = np.empty(n_e)
+        for i in range(n_e):
+            md = moments_delta(Ef[i] / a_ - 0.5 * (b[1] + b[0]) / a_, M).astype(np.complex128) * kern
+            rho[i] = np.real(blas.dot(1 + 0j, md, mu_c, M, threads) if blas is not None else md @ mu_c)
+        cpu_dos_s = time.perf_counter() - t0
+        blk["cpu_reference"] = {"value": float(n) * R * (M - 1) / cpu_rec_s, "unit": UNIT, "cores": threads,
+                                "kind": kind, "recursion_ms": cpu_rec_s * 1e3, "dos_loop_ms": cpu_dos_s * 1e3,
+                                "ms_per_dos": (cpu_rec_s + cpu_dos_s) * 1e3,
+                                "sample": "the full configuration: 4 vectors x M=512, then the DOS loop"}
+        blk["gpu_over_cpu_e2e"] = (cpu_rec_s + cpu_dos_s) / e2e_s
+        per_vec = [moment_parity(mu_h[r], mus[r]) for r in range(R)]
+        blk["parity_vs_reference"] = max(per_vec, key=lambda d: d["max_rel"])
+        blk["parity_vs_reference"]["vectors"] = R
+        blk["dos_max_abs_diff_over_max"] = float(np.max(np.abs(dos[:, 1] - rho)) / np.max(np.abs(rho)))
+    del op, v
+    return blk
+
+
 def run_ours(a):
     import ctypes
 
@@ -1082,6 +1263,13 @@ def run_ours(a):
             "max_abs_diff_vs_c128_over_mu0": float(np.max(np.abs(mu_f.cpu().numpy() - mu_h))
                                                    / np.max(np.abs(mu_h[:, 0]))),
             "note": "dtype KPM_C128F: every real as a float pair (~48 bits), FP32 pipe; opt-in"}
+    mu_fp64 = None
+    if a.dtype == "c128" and ff_products:
+        # the same recursion with every moment product in FP64 (KPM_MOMENTS_FP64=1): the strict
+        # all-FP64 form beside the default, timed on the same handle and vectors
+        blk, mu_fp64 = run_fp64_products(a, op, v, M, R, n, bytes_per_launch, hbm_peak, fma_rate.value, rec_fma,
+                                         world, mu_h)
+        line["c128_fp64_products"] = blk
     if a.dtype == "c128" and not a.no_time:
         line["time_evolution"] = run_time_evolution(a, op, n, L, prob, hbm_peak, world)
     if not a.no_setup:
@@ -1106,7 +1294,9 @@ def run_ours(a):
         barrier(world)
         with ClockSampler(local, enabled=not a.no_clocks) as clk_e2e:
             t0 = time.perf_counter()
-            e2e_steps = 1
+            # each pass is one step of the workload (all R vectors through the host-pointer call);
+            # at about 3.4 s a pass, the passes are capped so the run stays within a few minutes
+            e2e_steps = max(1, min(a.steps, a.e2e_max_steps))
             for _ in range(e2e_steps):
                 for r in range(R):
                     obv_gpu.rec_A_tab_gpu(data_p, idx_p, L, vs_p[r], out[r], M)
@@ -1114,6 +1304,7 @@ def run_ours(a):
             dt = max_over_ranks(time.perf_counter() - t0, world)
         assert np.allclose(out[:, 0].real, n, rtol=1e-6)
         line["e2e"] = {"value": float(n) * R * (M - 1) * e2e_steps * world / dt, "unit": UNIT,
+                       "steps": e2e_steps, "ms_per_step": 1e3 * dt / e2e_steps,
                        "h2d_bytes_per_step": int(R * (prob["data_kpm"].nbytes + prob["indices"].nbytes + n * 16)),
                        "d2h_bytes_per_step": int(R * M * 16),
                        "path": "obv_gpu.rec_A_tab_gpu -> exported rec_A_tab (host pointers, one vector per call)"}
@@ -1130,8 +1321,18 @@ def run_ours(a):
     if not a.no_kubo:
         torch.cuda.empty_cache()
         line["kubo"] = run_kubo(a, peaks, a.steps, a.warmup)
+    if not a.no_config1:
+        torch.cuda.empty_cache()
+        line["config1_dos"] = run_config1(a, world)
     if rank == 0 and world == 1 and not a.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(prob, a.cpu_seconds)
+        line["cpu_baseline"], mu_cpu = cpu_baseline(prob, a.cpu_seconds)
+        # parity at this configuration: the reference's own recursion on the host (same operator,
+        # same vector, seed 1000) against the GPU's vector 0, per order
+        line["parity_vs_reference"] = dict(moment_parity(mu_h[0], mu_cpu), vector="seed 1000 (GPU vector 0)",
+                                           kind=line["cpu_baseline"]["kind"],
+                                           gpu_path=line["fp64"]["moment_products"] if line.get("fp64") else a.dtype)
+        if mu_fp64 is not None:
+            line["c128_fp64_products"]["parity_vs_reference"] = moment_parity(mu_fp64[0], mu_cpu)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -191,6 +191,15 @@ int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int 
                                const double* c, const double* v, double* out, void* stream);
 
 /*
+ * Table of the commutator series: tab[r][m] = c[m] C_m (C_m of kpm_cheb_commutator_series
+ * for vector r; row m = 0 is c[0] C_0 = 0), m < M.  tab: device [R][M][n] c128 (each
+ * vector's table is the reference's [M, N] array).  dtype KPM_C128.
+ * Replaces rec_com_A_vec_tab (jclsquant/recurrence_functions.py:202-250).
+ */
+int kpm_cheb_commutator_table(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M, const double* c,
+                              const double* v, double* tab, void* stream);
+
+/*
  * Time-domain Kubo correlator sigma[r][j] = <U_c(t_j) | V1 U(t_j)>, j < len_t,
  * with U(t_0) = v, U_c(t_0) = sum_m c_fd[m] C_m (commutator series with V2),
  * and both advanced per time step by the series with c_u (M2 terms).
@@ -402,6 +411,15 @@ int kpm_last_status(void);
  * stops recording and drops what was recorded.
  * kpm_measure_fp64_fma_rate() times a kernel of independent FP64 FMA chains
  * on every SM and returns FMA/s (the FP64 ceiling of the complex128 path). */
+/* kpm_ell_test_timeout: a test hook of the bounded device waits (no counterpart in the
+ * reference).  Runs one producer-warp recursion step on h (one vector, zeroed workspace
+ * vectors) in which the producer arms the first shared-memory stage of every CTA for its
+ * bytes but issues none of its copies, with every wait bounded by budget_cycles SM clock
+ * cycles (1000 .. 2e9).  No copy is ever in flight for that stage, so the waits on it run
+ * out and the kernel takes its timeout path: it records KPM_ERR_TIMEOUT, waits (bounded)
+ * for the copies it did issue, and returns.  The call synchronises `stream` and returns
+ * what kpm_ell_check reads (KPM_ERR_TIMEOUT, then cleared); h stays usable. */
+int kpm_ell_test_timeout(kpm_ell* h, int64_t budget_cycles, void* stream);
 int kpm_ell_profile(kpm_ell* h, int enable);
 int kpm_ell_profile_read(kpm_ell* h, double* loop_ms, int64_t* step_launches, int64_t* rows_per_launch);
 int kpm_measure_fp64_fma_rate(double* fma_per_second, void* stream);

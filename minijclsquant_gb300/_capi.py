@@ -57,6 +57,7 @@ SIGNATURES = {
     "kpm_cheb_series": (_I, [_P, _I, _I, _I, _P, _P, _P, _P]),
     "kpm_time_evolve": (_I, [_P, _I, _I, _I, _P, _I, _P, _P, _P]),
     "kpm_cheb_commutator_series": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _P]),
+    "kpm_cheb_commutator_table": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _P]),
     "kpm_time_sigma": (_I, [_P, _P, _P, _I, _I, _P, _I, _P, _I, _I, _P, _P, _P]),
     "rec_A_tab": (None, [_P, _P, _I, _I, _P, _P, _I]),
     "rec_A_tab_2": (None, [_P, _P, _I, _I, _P, _P, _P, _I]),
@@ -89,6 +90,7 @@ SIGNATURES = {
     "kpm_batch_step_config": (_I, [_P, _I, _I, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I),
                                    ctypes.POINTER(ctypes.c_float), _P]),
     "kpm_batch_check": (_I, [_P, _P]),
+    "kpm_ell_test_timeout": (_I, [_P, _I64, _P]),
     "kpm_ell_profile": (_I, [_P, _I]),
     "kpm_ell_profile_read": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "kpm_measure_fp64_fma_rate": (_I, [ctypes.POINTER(_D), _P]),

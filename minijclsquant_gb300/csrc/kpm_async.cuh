@@ -9,10 +9,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "kpm_internal.cuh"
+
 namespace kpm {
 
-// ~1 s at 2 GHz: far beyond any legitimate wait for a few kilobytes.
-constexpr long long kWaitBudgetCycles = 2000000000LL;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -72,12 +72,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 
-// Wait for phase `parity` of `bar` to complete; false if the budget ran out.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+// Wait for phase `parity` of `bar` to complete; false if the budget (SM clock cycles; <= 0
+// means kWaitBudgetCycles) ran out.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity,
+                                                  long long budget = kWaitBudgetCycles) {
   if (mbar_try_wait(bar, parity)) return true;
+  if (budget <= 0) budget = kWaitBudgetCycles;
   const long long t0 = clock64();
   while (!mbar_try_wait(bar, parity)) {
-    if (clock64() - t0 > kWaitBudgetCycles) return false;
+    if (clock64() - t0 > budget) return false;
   }
   return true;
 }

@@ -245,6 +245,7 @@ StepParams batch_params(kpm_ell_s* h, bool f32) {
   p.n_pad = h->n_pad;
   p.a_half = make_double2(0.5, 0.0);
   p.err = h->err_flag;
+  p.wait_budget = kWaitBudgetCycles;
   p.vl = h->ws.vl.p;
   return p;
 }

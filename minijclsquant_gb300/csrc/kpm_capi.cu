@@ -14,7 +14,7 @@
 
 namespace kpm {
 int comm_series_packed(kpm_ell_s* h, kpm_ell_s* v, int Rg, int M, const double2* coef, const double2* x,
-                       double2* result, cudaStream_t s);
+                       double2* result, cudaStream_t s, double2* tab = nullptr, int r0 = 0);
 }
 
 using namespace kpm;
@@ -98,6 +98,7 @@ StepParams base_params(kpm_ell_s* h, bool f32) {
   p.a_half = make_double2(0.5, 0.0);
   p.b = make_double2(0.0, 0.0);
   p.err = h->err_flag;
+  p.wait_budget = kWaitBudgetCycles;
   return p;
 }
 
@@ -1035,6 +1036,29 @@ int kpm_cheb_commutator_series(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int 
   return KPM_OK;
 }
 
+int kpm_cheb_commutator_table(kpm_ell* h, kpm_ell* v_op, int dtype, int R, int M, const double* c,
+                              const double* v, double* tab, void* stream) {
+  if (!h || !v_op || !c || !v || !tab || R < 1 || M < 2) return KPM_ERR_INVALID_ARG;
+  if (v_op->n != h->n) return KPM_ERR_SHAPE;
+  KPM_TRY(check_dtype(dtype));
+  if (dtype != KPM_C128) return KPM_ERR_UNSUPPORTED;
+  cudaStream_t s = as_stream(stream);
+  const size_t row_bytes = (size_t)h->n * sizeof(double2);
+  for (int r = 0; r < R; ++r)  // row 0 of every table: c_0 C_0 with C_0 = 0
+    KPM_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char*>(tab) + (size_t)r * M * row_bytes, 0, row_bytes, s));
+  for (int r0 = 0; r0 < R;) {
+    const int Rg = pow2_group(R - r0);
+    const size_t vb = (size_t)h->n_pad * Rg * sizeof(double2);
+    KPM_TRY(ensure(h->ws.vl, vb));
+    KPM_TRY(pack_vectors(v, h->n, h->n_pad, R, r0, Rg, false, h->ws.vl.p, s));
+    KPM_TRY(comm_series_packed(h, v_op, Rg, M, reinterpret_cast<const double2*>(c),
+                               static_cast<const double2*>(h->ws.vl.p), nullptr, s, reinterpret_cast<double2*>(tab),
+                               r0));
+    r0 += Rg;
+  }
+  return KPM_OK;
+}
+
 int kpm_time_sigma(kpm_ell* h, kpm_ell* v1, kpm_ell* v2, int dtype, int R, const double* c_u, int M2,
                    const double* c_fd, int M, int len_t, const double* v, double* sigma, void* stream) {
   if (!h || !v1 || !v2 || !c_u || !c_fd || !v || !sigma || R < 1 || M < 2 || M2 < 2 || len_t < 1)
@@ -1106,6 +1130,34 @@ int kpm_ell_check(kpm_ell* h, void* stream) {
     return flag;
   }
   return KPM_OK;
+}
+
+int kpm_ell_test_timeout(kpm_ell* h, int64_t budget_cycles, void* stream) {
+  if (!h || budget_cycles < 1000 || budget_cycles > kWaitBudgetCycles) return KPM_ERR_INVALID_ARG;
+  cudaStream_t s = as_stream(stream);
+  const int occ = ws_ctas_f64(h->is_real, 1, 1, h->L, 2);
+  if (occ <= 0) return KPM_ERR_UNSUPPORTED;
+  const int64_t ntiles = h->n_pad / staged_tile_rows(false, 1, 1);
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
+  const size_t vb = (size_t)h->n_pad * sizeof(double2);
+  Workspace& ws = h->ws;
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  KPM_TRY(ensure(ws.part, (size_t)grid * sizeof(double2)));
+  KPM_CUDA_TRY(cudaMemsetAsync(ws.ta.p, 0, vb, s));
+  KPM_CUDA_TRY(cudaMemsetAsync(ws.tb.p, 0, vb, s));
+  KPM_CUDA_TRY(cudaMemsetAsync(ws.vl.p, 0, vb, s));
+  KPM_CUDA_TRY(cudaMemsetAsync(h->err_flag, 0, sizeof(int), s));
+  StepParams p = base_params(h, false);
+  p.tcur = ws.ta.p;
+  p.tout = ws.tb.p;
+  p.vl = ws.vl.p;
+  p.part = static_cast<double2*>(ws.part.p);
+  p.wait_budget = budget_cycles;
+  p.withhold_first = 1;
+  KPM_TRY(launch_ws_f64(h->is_real, 1, 1, p, grid, s));
+  return kpm_ell_check(h, stream);
 }
 
 int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid, float* step_us) {

@@ -11,6 +11,10 @@
 // and at m = 1: T_1 = H v, C_1 = V v, acc = c_1 C_1 (C_0 = 0).
 // The reference needs three SpMV launches and one axpy per order; here every
 // operator entry and every vector entry is touched once per order.
+//
+// The table form (TAB) serves rec_com_A_vec_tab (jclsquant/recurrence_functions.py:
+// 202-250): instead of the accumulator it writes c_m C_m as row m of the caller's
+// [R][M][n] table, straight from registers in the caller's unpacked layout.
 #include "kpm_cheb.cuh"
 
 namespace kpm {
@@ -30,9 +34,14 @@ struct CommParams {
   double2* acc;         // series accumulator
   const double2* coef;
   int m;
+  // TAB: out[(r0 + r) * tab_vstride + m * n + row] = c_m C_m for rows < n
+  double2* tab;
+  int64_t n;
+  int64_t tab_vstride;
+  int r0;
 };
 
-template <bool RH, bool RV, int R, bool FIRST>
+template <bool RH, bool RV, int R, bool FIRST, bool TAB>
 __global__ void __launch_bounds__(kBlock) comm_step_kernel(const CommParams p) {
   using MVH = typename MatV<double, RH>::type;
   using MVV = typename MatV<double, RV>::type;
@@ -77,6 +86,12 @@ __global__ void __launch_bounds__(kBlock) comm_step_kernel(const CommParams p) {
     }
     p.tout[vi] = pack(t);
     p.cout[vi] = pack(c);
+    if (TAB) {
+      if (row < p.n)
+        p.tab[(int64_t)(p.r0 + sub) * p.tab_vstride + (int64_t)p.m * p.n + row] =
+            make_double2(cm.x * c.re[0] - cm.y * c.im[0], cm.x * c.im[0] + cm.y * c.re[0]);
+      continue;
+    }
     double2 a;
     if (FIRST) {
       a = make_double2(cm.x * c.re[0] - cm.y * c.im[0], cm.x * c.im[0] + cm.y * c.re[0]);
@@ -91,10 +106,15 @@ __global__ void __launch_bounds__(kBlock) comm_step_kernel(const CommParams p) {
 
 template <bool RH, bool RV, int R>
 static int launch_comm_r(bool first, const CommParams& p, int grid, cudaStream_t s) {
-  if (first)
-    comm_step_kernel<RH, RV, R, true><<<grid, kBlock, 0, s>>>(p);
+  const bool tab = p.tab != nullptr;
+  if (first && tab)
+    comm_step_kernel<RH, RV, R, true, true><<<grid, kBlock, 0, s>>>(p);
+  else if (first)
+    comm_step_kernel<RH, RV, R, true, false><<<grid, kBlock, 0, s>>>(p);
+  else if (tab)
+    comm_step_kernel<RH, RV, R, false, true><<<grid, kBlock, 0, s>>>(p);
   else
-    comm_step_kernel<RH, RV, R, false><<<grid, kBlock, 0, s>>>(p);
+    comm_step_kernel<RH, RV, R, false, false><<<grid, kBlock, 0, s>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -123,8 +143,11 @@ static int launch_comm(bool rh, bool rv, int R, bool first, const CommParams& p,
 
 // Commutator series on one packed group: x ([n_pad][Rg] c128) in, result
 // written to `result` ([n_pad][Rg] c128).  Uses ws.ta..td of h.
+// With tab != nullptr the rows c_m C_m, m = 1 .. M-1, of vectors r0 .. r0+Rg-1 are written
+// into tab ([R][M][n] c128, unpacked) instead, and `result` is not touched; row 0
+// (c_0 C_0 = 0) is the caller's.
 int comm_series_packed(kpm_ell_s* h, kpm_ell_s* v, int Rg, int M, const double2* coef, const double2* x,
-                       double2* result, cudaStream_t s) {
+                       double2* result, cudaStream_t s, double2* tab, int r0) {
   const size_t vb = (size_t)h->n_pad * Rg * sizeof(double2);
   KPM_TRY(ensure(h->ws.tc, vb));
   KPM_TRY(ensure(h->ws.td, vb));
@@ -149,6 +172,10 @@ int comm_series_packed(kpm_ell_s* h, kpm_ell_s* v, int Rg, int M, const double2*
   p.n_pad = h->n_pad;
   p.coef = coef;
   p.acc = result;
+  p.tab = tab;
+  p.n = h->n;
+  p.tab_vstride = (int64_t)M * h->n;
+  p.r0 = r0;
   // m = 1: T_1 = H v -> t_b ; C_1 = V v -> c_b ; acc = c_1 C_1
   p.tcur = t_a;
   p.tout = t_b;

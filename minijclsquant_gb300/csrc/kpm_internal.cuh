@@ -30,6 +30,9 @@ constexpr int kBlock = 256;       // threads per CTA of every streaming kernel
 constexpr int kRowAlign = 512;    // n_pad is a multiple of this (and of every staged tile)
 constexpr int kMaxGroupR = 8;     // vectors advanced together by one launch
 constexpr int kChunk = 128;       // recursion steps whose moment partials are buffered
+// Budget of every bounded mbarrier wait: ~1 s at 2 GHz, far beyond any legitimate wait for a
+// few kilobytes.
+constexpr long long kWaitBudgetCycles = 2000000000LL;
 
 void set_last_cuda_error(cudaError_t e);
 
@@ -156,6 +159,12 @@ struct StepParams {
   // set): vl holds the float pairs of pack_left_ff, vl64 the same vectors in FP64
   int vl_ff;
   const void* vl64;
+  // Budget of the producer-warp kernel's mbarrier waits in SM clock cycles (base_params sets
+  // kWaitBudgetCycles, about 1 s).  withhold_first (test hook kpm_ell_test_timeout only): the
+  // producer arms the first stage's barrier for its bytes but issues no copy, so the waits on
+  // it run out and the kernel takes its timeout path.
+  long long wait_budget;
+  int withhold_first;
 };
 
 // Launch helpers implemented per precision (kpm_cheb_c128.cu, kpm_cheb_c64.cu).

@@ -131,17 +131,20 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       int issued = 0;
       for (int k = 0; k < my_count; ++k) {
         const int st = k % NST;
-        if (k >= NST && !mbar_wait_bounded(&empty[st], (uint32_t)(((k / NST) - 1) & 1))) {
+        if (k >= NST && !mbar_wait_bounded(&empty[st], (uint32_t)(((k / NST) - 1) & 1), p.wait_budget)) {
           atomicExch(p.err, KPM_ERR_TIMEOUT);
           break;
         }
         fence_proxy_async_shared();
-        issue_tile(tc, smem + st * stage_b, &full[st], tile_of(k) * TILE, TPR * (int)sizeof(Raw), pol);
+        if (k == 0 && p.withhold_first)  // test hook: the stage is armed, its copies never issued
+          mbar_arrive_expect_tx(&full[st], tc.tx_bytes);
+        else
+          issue_tile(tc, smem + st * stage_b, &full[st], tile_of(k) * TILE, TPR * (int)sizeof(Raw), pol);
         issued = k + 1;
       }
       // copies of the last stages may still be landing: wait for them before leaving
       for (int q = issued > NST ? issued - NST : 0; q < issued; ++q)
-        (void)mbar_wait_bounded(&full[q % NST], (uint32_t)((q / NST) & 1));
+        (void)mbar_wait_bounded(&full[q % NST], (uint32_t)((q / NST) & 1), p.wait_budget);
     }
     return;
   }
@@ -197,7 +200,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
 
   for (int k = 0; k < my_count; ++k) {
     const int st = k % NST;
-    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / NST) & 1));
+    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / NST) & 1), p.wait_budget);
     ok = __all_sync(0xffffffffu, ok);
     if (!ok && !dead) {
       if (lane == 0) atomicExch(p.err, KPM_ERR_TIMEOUT);

@@ -243,6 +243,21 @@ def cheb_commutator_series(op: DeviceELL, vop: DeviceELL, M: int, c, v, dtype="c
     return _finish(out, squeeze, was_np)
 
 
+def cheb_commutator_table(op: DeviceELL, vop: DeviceELL, M: int, c, v, dtype="c128", stream=None):
+    """tab[m] = c[m] C_m, m < M, of the commutator recursion (rec_com_A_vec_tab): [M, n] for
+    one vector, [R, M, n] for R vectors."""
+    M = int(M)
+    if M < 2:
+        raise ValueError("M must be >= 2")
+    tv, R, squeeze, was_np = _vectors(v, op.n)
+    tc = _coef(c, M, tv.device)
+    tab = torch.empty((R, M, op.n), dtype=torch.complex128, device=tv.device)
+    st = _capi.lib().kpm_cheb_commutator_table(op.handle, vop.handle, _capi.dtype_code(dtype), R, M, tc.data_ptr(),
+                                               tv.data_ptr(), tab.data_ptr(), _stream_ptr(stream))
+    _capi.check(st, "kpm_cheb_commutator_table")
+    return _finish(tab, squeeze, was_np)
+
+
 def ell_dot(op: DeviceELL, a, b, x, y, stream=None):
     """y <- b*y + a*H x on the GPU; y is updated in place (numpy or CUDA tensor)."""
     tx, R, squeeze, _ = _vectors(x, op.n)

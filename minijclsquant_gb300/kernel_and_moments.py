@@ -63,12 +63,43 @@ def moments_FD_T(Ef, T_mod, N):
     return mu
 
 
+def moments_FD(N, FD):
+    """Chebyshev moments of a tabulated occupation FD(E) on linspace(-1 + 1e-3, 1 - 1e-3, len(FD))
+    by Simpson quadrature, the n = 0 weight halved (jclsquant/kernel_and_moments.py:107-115)."""
+    from scipy.integrate import simpson
+
+    FD = np.asarray(FD)
+    E = np.linspace(-1 + 1e-3, 1 - 1e-3, len(FD))
+    w = FD / (pi * np.sqrt(1 - E ** 2))
+    theta = np.arccos(E)
+    mu = np.zeros(N)
+    for m in range(N):
+        mu[m] = 2 * simpson(w * np.cos(m * theta), x=E, dx=np.abs(E[1] - E[0]))
+    mu[0] = mu[0] / 2
+    return mu
+
+
 def moments_Gmas(Ef, N):
     """Retarded Green's function moments (jclsquant/kernel_and_moments.py:47-54)."""
     n = np.arange(1, N)
     s = np.sqrt(1 - Ef ** 2)
     body = -2j * np.exp(-1j * n * np.arccos(Ef)) / s
     return np.concatenate((np.array([-1j / s]), body))
+
+
+def moments_Gmas_2(Ef, broadening, N):
+    """Retarded Green's function moments at the complex energy z = Ef + i*broadening
+    (jclsquant/kernel_and_moments.py:33-41): [-i/s, 2 (z - i s)^n / (i s)] with s = sqrt(1 - z^2)."""
+    z = Ef + 1j * broadening
+    s = np.sqrt(1 - z ** 2)
+    n = np.arange(1, N)
+    body = 2 * (z - 1j * s) ** n / (1j * s)
+    return np.concatenate((np.array([-1j / s]), body))
+
+
+def moments_delta_2(Ef, broadening, M):
+    """Lorentzian-broadened delta moments, -Im G+ / pi (jclsquant/kernel_and_moments.py:43-44)."""
+    return -np.imag(moments_Gmas_2(Ef, broadening, M)) / np.pi
 
 
 def moments_Gmin(Ef, N):

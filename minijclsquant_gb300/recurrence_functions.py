@@ -69,3 +69,19 @@ def rec_com_A_vec(M, A, V=None, moments_kernel=None, v=None):
         print("You must introduce a vector.")
         return None
     return device.cheb_commutator_series(A.device(), V.device(), M, moments_kernel, v)
+
+
+def rec_com_A_vec_tab(M, A, V=None, moments_kernel=None, v=None):
+    """Table of the commutator series, C_tab[m] = c_m C_m, an [M, N] array
+    (jclsquant/recurrence_functions.py:202-250); [R, M, N] for R vectors."""
+    if V is None:
+        print("You must introduce kpm renormalized velocity .")
+        return None
+    if v is None:
+        print("You must introduce a vector.")
+        return None
+    if moments_kernel is None:
+        # the reference indexes moments_kernel[0] unconditionally
+        raise TypeError("'NoneType' object is not subscriptable")
+    _check_order(M)
+    return device.cheb_commutator_table(A.device(), V.device(), M, moments_kernel, v)

@@ -29,7 +29,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 REF_DIR = os.path.join(HERE, "_ref")
 ORACLE_SO = os.path.join(BUILD_DIR, "libkpm_oracle.so")
-REFERENCE_ROOT = "/root/reference"
+# The reference source tree (read-only); KPM_REFERENCE_ROOT points elsewhere if it lives there.
+REFERENCE_ROOT = os.environ.get("KPM_REFERENCE_ROOT", "/root/reference")
 REF_PYX = {
     "blas_funs": os.path.join(REFERENCE_ROOT, "jclsquant", "cython_modules", "blas_funs.pyx"),
     "Extra_funs": os.path.join(REFERENCE_ROOT, "jclsquant", "cython_modules", "Extra_funs.pyx"),

@@ -179,9 +179,11 @@ int oracle_rec_A_vec(int M, const zc* data, const int32_t* indices, int len_row,
  * C_m = 2 A C_{m-1} - C_{m-2} + 2 V T_{m-1}; A and V share one ELL pattern.
  * Follows recurrence_functions.py:146-196 (rec_com_A_vec), including its
  * update order: C0 <- 2 A C1 - C0; C0 <- 2 V T1 + C0; swap; then the T step. */
-int oracle_rec_com_A_vec(int M, const zc* data_a, const zc* data_v,
-                         const int32_t* indices, int len_row, int n, const zc* c,
-                         const zc* v, zc* out, int threads) {
+/* out != NULL: the series; tab != NULL: the table tab[m*n + i] = c_m C_m,i of
+ * rec_com_A_vec_tab (recurrence_functions.py:202-250), row 0 = c_0 C_0 = 0. */
+static int com_recursion(int M, const zc* data_a, const zc* data_v, const int32_t* indices,
+                         int len_row, int n, const zc* c, const zc* v, zc* out, zc* tab,
+                         int threads) {
   if (M < 2 || n < 1 || len_row < 1) return -1;
   zc* T0 = (zc*)malloc(sizeof(zc) * (size_t)n);
   zc* T1 = (zc*)calloc((size_t)n, sizeof(zc));
@@ -191,17 +193,38 @@ int oracle_rec_com_A_vec(int M, const zc* data_a, const zc* data_v,
   memcpy(T0, v, sizeof(zc) * (size_t)n);
   oracle_aAxby(1.0, 0.0, 0.0, 0.0, v, T1, data_a, indices, len_row, n, threads);
   oracle_aAxby(1.0, 0.0, 0.0, 0.0, v, C1, data_v, indices, len_row, n, threads);
-  for (int i = 0; i < n; ++i) out[i] = c[1] * C1[i];
+  if (out)
+    for (int i = 0; i < n; ++i) out[i] = c[1] * C1[i];
+  if (tab)
+    for (int i = 0; i < n; ++i) {
+      tab[i] = c[0] * C0[i];
+      tab[(size_t)n + i] = c[1] * C1[i];
+    }
   for (int m = 2; m < M; ++m) {
     oracle_aAxby(2.0, 0.0, -1.0, 0.0, C1, C0, data_a, indices, len_row, n, threads);
     oracle_aAxby(2.0, 0.0, 1.0, 0.0, T1, C0, data_v, indices, len_row, n, threads);
     zc* t = C0; C0 = C1; C1 = t;
     oracle_aAxby(2.0, 0.0, -1.0, 0.0, T1, T0, data_a, indices, len_row, n, threads);
     t = T0; T0 = T1; T1 = t;
-    oracle_axpy2(creal(c[m]), cimag(c[m]), 1.0, 0.0, C1, out, n, threads);
+    if (out) oracle_axpy2(creal(c[m]), cimag(c[m]), 1.0, 0.0, C1, out, n, threads);
+    if (tab)
+      for (int i = 0; i < n; ++i) tab[(size_t)m * n + i] = c[m] * C1[i];
   }
   free(T0); free(T1); free(C0); free(C1);
   return 0;
+}
+
+int oracle_rec_com_A_vec(int M, const zc* data_a, const zc* data_v,
+                         const int32_t* indices, int len_row, int n, const zc* c,
+                         const zc* v, zc* out, int threads) {
+  return com_recursion(M, data_a, data_v, indices, len_row, n, c, v, out, NULL, threads);
+}
+
+/* rec_com_A_vec_tab (recurrence_functions.py:202-250): tab is [M][n]. */
+int oracle_rec_com_A_vec_tab(int M, const zc* data_a, const zc* data_v,
+                             const int32_t* indices, int len_row, int n, const zc* c,
+                             const zc* v, zc* tab, int threads) {
+  return com_recursion(M, data_a, data_v, indices, len_row, n, c, v, NULL, tab, threads);
 }
 
 /* Time-domain Kubo sigma(t_j) = <U_c(t_j) | V1 U(t_j)> (without the final

@@ -34,6 +34,7 @@ def lib():
         c.oracle_rec_A_tab2v_2.argtypes = [I, P, P, I, I, P, P, P, P, I]
         c.oracle_rec_A_vec.argtypes = [I, P, P, I, I, P, P, P, I]
         c.oracle_rec_com_A_vec.argtypes = [I, P, P, P, I, I, P, P, P, I]
+        c.oracle_rec_com_A_vec_tab.argtypes = [I, P, P, P, I, I, P, P, P, I]
         c.oracle_for_time_sigma.argtypes = [P, P, P, P, I, I, P, P, I, P, P, I, I, I]
         c.oracle_max_threads.restype = I
         c.oracle_adjoint_grad.argtypes = [I, P, P, I, I, P, P, P]
@@ -135,6 +136,17 @@ def rec_com_A_vec(M, data_a, data_v, indices, len_row, c, v, threads=None):
                                       int(len_row), v.size, c.ctypes.data, v.ctypes.data, out.ctypes.data,
                                       threads or default_threads()), "rec_com_A_vec")
     return out
+
+
+def rec_com_A_vec_tab(M, data_a, data_v, indices, len_row, c, v, threads=None):
+    """Commutator table C_tab[m] = c_m C_m, [M, n] (recurrence_functions.py:202-250)."""
+    data_a, data_v = _c(data_a, np.complex128), _c(data_v, np.complex128)
+    indices, c, v = _c(indices, np.int32), _c(c, np.complex128), _c(v, np.complex128)
+    tab = np.zeros((int(M), v.size), dtype=np.complex128)
+    _check(lib().oracle_rec_com_A_vec_tab(int(M), data_a.ctypes.data, data_v.ctypes.data, indices.ctypes.data,
+                                          int(len_row), v.size, c.ctypes.data, v.ctypes.data, tab.ctypes.data,
+                                          threads or default_threads()), "rec_com_A_vec_tab")
+    return tab
 
 
 def for_time_sigma(data_h, data_v1, data_v2, indices, len_row, c_u, c_fd, len_t, v, M, M2, threads=None):

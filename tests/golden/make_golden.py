@@ -174,6 +174,9 @@ def main():
 
     time_evolution_case(ref)
     modifiers_case(ref)
+    commutator_table_case(ref)
+    two_vector_dos_case(ref)
+    kernels_more_case(ref)
 
 
 def time_evolution_case(ref):
@@ -241,7 +244,76 @@ def modifiers_case(ref):
     save("modifiers_6x5", **out)
 
 
-CASES = {"time_evolution_6x5": time_evolution_case, "modifiers_6x5": modifiers_case}
+def commutator_table_case(ref):
+    """10. the commutator table rec_com_A_vec_tab (jclsquant/recurrence_functions.py:202-250):
+    C_tab[m] = c_m C_m on a graphene lattice with complex (Peierls-like) hoppings and open
+    edges, V the rescaled velocity H o dx / a (modifier_velocity_bounds)."""
+    rf = ref.recurrence_functions
+    km = ref.kernel_and_moments
+    arr = lattice.honeycomb_arrays(5, 4, t=-2.7, W=0.6, seed=17, periodic=False)
+    phase = np.exp(1j * 0.4 * np.real(arr["dy"]) / 0.142)
+    arr_c = dict(arr, data=np.where(np.real(arr["dy"]) != 0, arr["data"] * phase, arr["data"]))
+    dx = lattice.to_csr(dict(arr, data=arr["dx"]))
+    dy = lattice.to_csr(dict(arr, data=arr["dy"]))
+    H = ref.ell_matrix.ell_matrix(lattice.to_csr(arr_c), dx, dy, None)
+    H_kpm = H.modifier(ref.modifiers.modifier_bounds)
+    V = H.modifier(ref.modifiers.modifier_velocity_bounds, "x")
+    n = int(H.shape[0])
+    M = 20
+    coef = (km.moments_FD_T0(-0.2, M) * km.JacksonKernel(M)).astype(np.complex128)
+    v = ref.observables.random_vector_generator(n, 808)
+    tab = rf.rec_com_A_vec_tab(M, H_kpm, V, coef, v)
+    save("commutator_table_5x4", data_kpm=H_kpm.data, v_data=V.data, indices=H.indices, len_row=np.int64(H.len_row),
+         n=np.int64(n), M=np.int64(M), coef=coef, v=v, tab=tab, series=rf.rec_com_A_vec(M, H_kpm, V, coef, v))
+
+
+def two_vector_dos_case(ref):
+    """11. the two-vector DOS kpm_n_dos_n (jclsquant/observables.py:59-120) with and without
+    a projector (an ELL matrix applied to the bra vector by its .dot), with bounds=True and
+    bounds=False (H already rescaled).  kpm_dos_2_gpu (jclsquant/observables_gpu.py:46-93)
+    computes the same quantity through the device recursion of the same maths, so these
+    outputs pin both entry points."""
+    ob = ref.observables
+    arr = lattice.honeycomb_arrays(8, 8, t=-2.7, W=0.5, seed=1234)
+    H = ref.ell_matrix.ell_matrix(lattice.to_csr(arr))
+    n = int(H.shape[0])
+    M = 64
+    v_l = ob.random_vector_generator(n, 31)
+    v_r = ob.random_vector_generator(n, 32)
+    import scipy.sparse as sp
+
+    # projector on sublattice A (even sites), weighted 0.5..1.5 per site
+    w = np.where(np.arange(n) % 2 == 0, 0.5 + np.linspace(0, 1, n), 0.0).astype(np.complex128)
+    P = ref.ell_matrix.ell_matrix(sp.csr_matrix(sp.diags(w)).tocsr())
+    plain = ob.kpm_n_dos_n(H, M, v_l, v_r)
+    proj = ob.kpm_n_dos_n(H, M, v_l, v_r, True, P)
+    H_kpm = H.modifier(ref.modifiers.modifier_bounds)
+    # bounds=False: the caller passes the rescaled operator (with the original bounds kept
+    # on the object for the energy grid, as the reference reads H.bounds)
+    H_kpm.bounds = H.bounds
+    nob = ob.kpm_n_dos_n(H_kpm, M, v_l, v_r, False)
+    save("two_vector_dos_8x8", data=H.data, indices=H.indices, valid=H.valid_row_values, bounds=np.asarray(H.bounds),
+         len_row=np.int64(H.len_row), n=np.int64(n), M=np.int64(M), v_l=v_l, v_r=v_r, proj_data=P.data,
+         proj_indices=P.indices, proj_len_row=np.int64(P.len_row), dos=plain, dos_proj=proj, dos_nobounds=nob)
+
+
+def kernels_more_case(ref):
+    """12. the broadened Green's function and delta moments and the tabulated Fermi-Dirac
+    moments (jclsquant/kernel_and_moments.py:33-44, 107-115)."""
+    km = ref.kernel_and_moments
+    E = np.linspace(-0.95, 0.95, 5)
+    eta = np.array([1e-3, 0.02, 0.1])
+    g2 = np.stack([np.stack([km.moments_Gmas_2(e, b, 48) for b in eta]) for e in E])
+    d2 = np.stack([np.stack([km.moments_delta_2(e, b, 48) for b in eta]) for e in E])
+    grid = np.linspace(-1 + 1e-3, 1 - 1e-3, 401)
+    fd_tab = np.stack([1 / (1 + np.exp((grid - ef) / kt)) for ef, kt in ((0.0, 0.02), (-0.3, 0.1), (0.6, 0.005))])
+    fd = np.stack([km.moments_FD(64, f) for f in fd_tab])
+    save("kernels_more", E=E, eta=eta, gmas2=g2, delta2=d2, fd_tab=fd_tab, moments_fd=fd)
+
+
+CASES = {"time_evolution_6x5": time_evolution_case, "modifiers_6x5": modifiers_case,
+         "commutator_table_5x4": commutator_table_case, "two_vector_dos_8x8": two_vector_dos_case,
+         "kernels_more": kernels_more_case}
 
 
 if __name__ == "__main__":

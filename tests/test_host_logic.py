@@ -76,6 +76,21 @@ def test_kernels_match_reference():
     assert np.allclose(tab, z["delta"], rtol=1e-14, atol=1e-14)
 
 
+def test_broadened_and_tabulated_moments_match_reference():
+    """moments_Gmas_2, moments_delta_2 and moments_FD (jclsquant/kernel_and_moments.py:33-44,
+    107-115) against the reference's own outputs."""
+    z = golden("kernels_more")
+    for i, e in enumerate(z["E"]):
+        for j, b in enumerate(z["eta"]):
+            g = km.moments_Gmas_2(e, b, 48)
+            assert g.dtype == np.complex128 and g.shape == (48,)
+            assert np.allclose(g, z["gmas2"][i, j], rtol=1e-13, atol=1e-13 * np.max(np.abs(z["gmas2"][i, j])))
+            assert np.allclose(km.moments_delta_2(e, b, 48), z["delta2"][i, j], rtol=1e-13,
+                               atol=1e-13 * np.max(np.abs(z["delta2"][i, j])))
+    for k, f in enumerate(z["fd_tab"]):
+        assert np.allclose(km.moments_FD(64, f), z["moments_fd"][k], rtol=1e-13, atol=1e-15)
+
+
 @pytest.mark.parametrize("case", ["honeycomb_8x8", "ref_graphene_256", "irregular_300", "honeycomb_64x64"])
 def test_dos_reconstruction_matches_reference(case):
     z = golden(case)

@@ -48,6 +48,37 @@ def test_oracle_other_recursions_match_reference():
     assert np.max(np.abs(sig - x["sigma"])) <= 1e-11 * np.max(np.abs(x["sigma"]))
 
 
+def test_oracle_commutator_table_matches_reference():
+    z = golden("commutator_table_5x4")
+    tab = oracle.rec_com_A_vec_tab(int(z["M"]), z["data_kpm"], z["v_data"], z["indices"], int(z["len_row"]),
+                                   z["coef"], z["v"])
+    assert np.max(np.abs(tab - z["tab"])) <= 1e-13 * np.max(np.abs(z["tab"]))
+    ser = oracle.rec_com_A_vec(int(z["M"]), z["data_kpm"], z["v_data"], z["indices"], int(z["len_row"]), z["coef"],
+                               z["v"])
+    assert np.max(np.abs(ser - z["series"])) <= 1e-13 * np.max(np.abs(z["series"]))
+
+
+def test_oracle_two_vector_dos_matches_reference():
+    """The two-vector DOS fixture (kpm_n_dos_n with and without a projector) rebuilt from the
+    oracle's rec_A_tab2v and the host reconstruction."""
+    from minijclsquant_gb300.ell_matrix import ell_matrix
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from minijclsquant_gb300.observables import dos_from_moments
+
+    z = golden("two_vector_dos_8x8")
+    L, M = int(z["len_row"]), int(z["M"])
+    H = ell_matrix.from_ell(z["data"], z["indices"], L, bounds=z["bounds"], valid_row_values=z["valid"])
+    dk = H.modifier(modifier_bounds).data
+    mu = oracle.rec_A_tab2v(M, dk, z["indices"], L, z["v_l"], z["v_r"])
+    got = dos_from_moments(mu, z["bounds"], M)
+    assert np.max(np.abs(got[:, 1] - z["dos"][:, 1])) <= 1e-12 * np.max(np.abs(z["dos"][:, 1]))
+    pl = np.zeros_like(z["v_l"])
+    oracle.aAxby(1.0, 0.0, z["v_l"], pl, z["proj_data"], z["proj_indices"], int(z["proj_len_row"]))
+    mu_p = oracle.rec_A_tab2v(M, dk, z["indices"], L, pl, z["v_r"])
+    got_p = dos_from_moments(mu_p, z["bounds"], M)
+    assert np.max(np.abs(got_p[:, 1] - z["dos_proj"][:, 1])) <= 1e-12 * np.max(np.abs(z["dos_proj"][:, 1]))
+
+
 def test_oracle_time_evolution_matches_reference():
     z = golden("time_evolution_6x5")
     U, Uc = oracle.for_time(z["data_kpm"], z["indices"], int(z["len_row"]), z["c"], int(z["len_t"]), z["U0"],

@@ -237,6 +237,29 @@ int kpm_adjoint_backward(kpm_ell* h, const double* c, double* grad, void* stream
  * relative to the FP64 gradient). */
 int kpm_adjoint_backward_ex(kpm_ell* h, const double* c, double* grad, int dtype, void* stream);
 
+/* ---- vector tables (reverse mode of the Kubo-Greenwood conductivity) -------
+ * No counterpart in the reference.  A table is M rows of n c128 values (row m at
+ * tab + 2 m n doubles), one vector, device memory; h is the rescaled H, s_op a second
+ * operator of the same size (e.g. the velocity V = -i H o dx of modifier_velocity,
+ * jclsquant/modifiers.py:56-79).  Stream-ordered; nothing is allocated.
+ * kpm_cheb_table: tab[m] = T_m(H) v, m < M (the recursion of rec_A_tab,
+ *   jclsquant/recurrence_functions.py:9-40, with every vector kept); with s_op also
+ *   stab[m] = S T_m(H) v from the same gathers (stab must then be given, else NULL).
+ * kpm_cheb_clenshaw_table: the reverse recursion lam_k = S z_k + 2 H lam_{k+1} - lam_{k+2}
+ *   (k = M-1 .. 1), lam_0 = S z_0 + H lam_1 - lam_2, lam_M = lam_{M+1} = 0, all rows kept
+ *   (S = identity when s_op is NULL).  lam_0 = sum_k T_k(H) S z_k (Clenshaw), and for a
+ *   functional Re sum_k (S z_k)^H T_k(H) w the rows are its adjoint vectors: the derivative
+ *   by the entry (i, j) of H is sum_{k <= M-2} c_k conj(lam_{k+1}[i]) (T_k(H) w)[j], c_0 = 1,
+ *   c_k = 2 (kpm_ell_slot_sum).
+ * kpm_ell_slot_sum: per stored entry of h (reference AoS layout [n][len_row], c128),
+ *   out[i][s] (+)= sum_{k<K} coef[k] conj(A[k][i]) B[k][col(i, s)], rows of A and B lda, ldb
+ *   complex numbers apart (>= n); coef device [K] doubles or NULL (all 1); accumulate != 0
+ *   adds to out.  len_row <= 16. */
+int kpm_cheb_table(kpm_ell* h, kpm_ell* s_op, int M, const double* v, double* tab, double* stab, void* stream);
+int kpm_cheb_clenshaw_table(kpm_ell* h, kpm_ell* s_op, int M, const double* z, double* lam, void* stream);
+int kpm_ell_slot_sum(kpm_ell* h, int K, const double* coef, const double* A, int64_t lda, const double* B,
+                     int64_t ldb, int accumulate, double* out, void* stream);
+
 /* ---- Kubo-Greenwood moment matrix on the tensor cores ---------------------
  * No counterpart in the reference (its conductivity is the time-domain
  * correlator of for_time_sigma); velocity conventions are those of
@@ -304,13 +327,18 @@ int kpm_batch_check(kpm_batch* b, void* stream);
  * (data: n*len_row c128, indices: n*len_row int32, already rescaled).
  * v: device [n] c128; mu: device [M] c128.  Nothing is allocated: the working
  * vectors and moment partials live in one fixed file-scope device array
- * (about 33 MiB, held by every GPU that loads the library until exit), so
- * n <= 1,048,576 sites; larger n returns KPM_ERR_TOO_LARGE.
- * The first call on a device looks up that array's address (once per
- * device): make it outside any stream capture.  All calls on a device share
- * the array: calls that overlap on the GPU race; serialise them.  The call
- * waits for its stream to finish so it can return KPM_ERR_INDEX when a column
- * index is outside [0, n) (such entries are skipped).
+ * (about 33 MiB), so n <= 1,048,576 sites; larger n returns KPM_ERR_TOO_LARGE.
+ * Under lazy module loading (the CUDA default) that array is reserved in a
+ * CUDA context when the library's device code is first used there, which for
+ * a caller of this entry point alone is its first call: make that call at
+ * set-up time (while the device has room for the array) and outside any
+ * stream capture, or set CUDA_MODULE_LOADING=EAGER.  The context then holds
+ * the array until it is destroyed.  Each call finds the array's address in
+ * the context current on the calling thread, so call with the context that
+ * should run the work current.  All calls in a context share the array:
+ * calls that overlap on the GPU race; serialise them.  The call waits for its
+ * stream to finish so it can return KPM_ERR_INDEX when a column index is
+ * outside [0, n) (such entries are skipped).
  */
 int kpm_cheb_moments_noalloc(const double* data, const int32_t* indices, int len_row, int64_t n,
                              const double* v, int M, double* mu, void* stream);

@@ -68,6 +68,9 @@ SIGNATURES = {
     "kpm_adjoint_forward": (_I, [_P, _I, _I, _I, _P, _P, _P]),
     "kpm_adjoint_backward": (_I, [_P, _P, _P, _P]),
     "kpm_cheb_moments_noalloc": (_I, [_P, _P, _I, _I64, _P, _I, _P, _P]),
+    "kpm_cheb_table": (_I, [_P, _P, _I, _P, _P, _P, _P]),
+    "kpm_cheb_clenshaw_table": (_I, [_P, _P, _I, _P, _P, _P]),
+    "kpm_ell_slot_sum": (_I, [_P, _I, _P, _P, _I64, _P, _I64, _I, _P, _P]),
     "kpm_mu_nm": (_I, [_P, _P, _I, _I, _P, _P, _P]),
     "kpm_mu_contract": (_I, [_P, _P, _I64, _I64, _I, _D, _I, _P, _P]),
     "kpm_batch_create": (_I, [ctypes.POINTER(_P), _I, _P, _I, _P, _P, _P]),

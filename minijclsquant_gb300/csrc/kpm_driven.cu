@@ -47,6 +47,268 @@ __device__ __forceinline__ double2 cexp2(double2 z) {
   const double e = z.x == 0.0 ? 1.0 : exp(z.x);  // a pure phase (real pulse parameters): exp(0) = 1
   return make_double2(e * c, e * s);
 }
+// (sin, cos)(2 pi k / 256), k = 0 .. 255: each entry is the exact value rounded to the nearest
+// double (computed in 60-digit arithmetic; a CPU test recomputes every entry).  A file-scope
+// device constant: the kernels read it directly, so a light update needs no set-up.
+__device__ const double2 g_sincos_tab[256] = {
+    {0.0, 0x1.0000000000000p+0},
+    {0x1.92155f7a3667ep-6, 0x1.ffd886084cd0dp-1},
+    {0x1.91f65f10dd814p-5, 0x1.ff621e3796d7ep-1},
+    {0x1.2d52092ce19f6p-4, 0x1.fe9cdad01883ap-1},
+    {0x1.917a6bc29b42cp-4, 0x1.fd88da3d12526p-1},
+    {0x1.f564e56a9730ep-4, 0x1.fc26470e19fd3p-1},
+    {0x1.2c8106e8e613ap-3, 0x1.fa7557f08a517p-1},
+    {0x1.5e214448b3fc6p-3, 0x1.f8764fa714ba9p-1},
+    {0x1.8f8b83c69a60bp-3, 0x1.f6297cff75cb0p-1},
+    {0x1.c0b826a7e4f63p-3, 0x1.f38f3ac64e589p-1},
+    {0x1.f19f97b215f1bp-3, 0x1.f0a7efb9230d7p-1},
+    {0x1.111d262b1f677p-2, 0x1.ed740e7684963p-1},
+    {0x1.294062ed59f06p-2, 0x1.e9f4156c62ddap-1},
+    {0x1.4135c94176601p-2, 0x1.e6288ec48e112p-1},
+    {0x1.58f9a75ab1fddp-2, 0x1.e212104f686e5p-1},
+    {0x1.7088530fa459fp-2, 0x1.ddb13b6ccc23cp-1},
+    {0x1.87de2a6aea963p-2, 0x1.d906bcf328d46p-1},
+    {0x1.9ef7943a8ed8ap-2, 0x1.d4134d14dc93ap-1},
+    {0x1.b5d1009e15cc0p-2, 0x1.ced7af43cc773p-1},
+    {0x1.cc66e9931c45ep-2, 0x1.c954b213411f5p-1},
+    {0x1.e2b5d3806f63bp-2, 0x1.c38b2f180bdb1p-1},
+    {0x1.f8ba4dbf89abap-2, 0x1.bd7c0ac6f952ap-1},
+    {0x1.073879922ffeep-1, 0x1.b728345196e3ep-1},
+    {0x1.11eb3541b4b23p-1, 0x1.b090a58150200p-1},
+    {0x1.1c73b39ae68c8p-1, 0x1.a9b66290ea1a3p-1},
+    {0x1.26d054cdd12dfp-1, 0x1.a29a7a0462782p-1},
+    {0x1.30ff7fce17035p-1, 0x1.9b3e047f38741p-1},
+    {0x1.3affa292050b9p-1, 0x1.93a22499263fbp-1},
+    {0x1.44cf325091dd6p-1, 0x1.8bc806b151741p-1},
+    {0x1.4e6cabbe3e5e9p-1, 0x1.83b0e0bff976ep-1},
+    {0x1.57d69348ceca0p-1, 0x1.7b5df226aafafp-1},
+    {0x1.610b7551d2cdfp-1, 0x1.72d0837efff96p-1},
+    {0x1.6a09e667f3bcdp-1, 0x1.6a09e667f3bcdp-1},
+    {0x1.72d0837efff96p-1, 0x1.610b7551d2cdfp-1},
+    {0x1.7b5df226aafafp-1, 0x1.57d69348ceca0p-1},
+    {0x1.83b0e0bff976ep-1, 0x1.4e6cabbe3e5e9p-1},
+    {0x1.8bc806b151741p-1, 0x1.44cf325091dd6p-1},
+    {0x1.93a22499263fbp-1, 0x1.3affa292050b9p-1},
+    {0x1.9b3e047f38741p-1, 0x1.30ff7fce17035p-1},
+    {0x1.a29a7a0462782p-1, 0x1.26d054cdd12dfp-1},
+    {0x1.a9b66290ea1a3p-1, 0x1.1c73b39ae68c8p-1},
+    {0x1.b090a58150200p-1, 0x1.11eb3541b4b23p-1},
+    {0x1.b728345196e3ep-1, 0x1.073879922ffeep-1},
+    {0x1.bd7c0ac6f952ap-1, 0x1.f8ba4dbf89abap-2},
+    {0x1.c38b2f180bdb1p-1, 0x1.e2b5d3806f63bp-2},
+    {0x1.c954b213411f5p-1, 0x1.cc66e9931c45ep-2},
+    {0x1.ced7af43cc773p-1, 0x1.b5d1009e15cc0p-2},
+    {0x1.d4134d14dc93ap-1, 0x1.9ef7943a8ed8ap-2},
+    {0x1.d906bcf328d46p-1, 0x1.87de2a6aea963p-2},
+    {0x1.ddb13b6ccc23cp-1, 0x1.7088530fa459fp-2},
+    {0x1.e212104f686e5p-1, 0x1.58f9a75ab1fddp-2},
+    {0x1.e6288ec48e112p-1, 0x1.4135c94176601p-2},
+    {0x1.e9f4156c62ddap-1, 0x1.294062ed59f06p-2},
+    {0x1.ed740e7684963p-1, 0x1.111d262b1f677p-2},
+    {0x1.f0a7efb9230d7p-1, 0x1.f19f97b215f1bp-3},
+    {0x1.f38f3ac64e589p-1, 0x1.c0b826a7e4f63p-3},
+    {0x1.f6297cff75cb0p-1, 0x1.8f8b83c69a60bp-3},
+    {0x1.f8764fa714ba9p-1, 0x1.5e214448b3fc6p-3},
+    {0x1.fa7557f08a517p-1, 0x1.2c8106e8e613ap-3},
+    {0x1.fc26470e19fd3p-1, 0x1.f564e56a9730ep-4},
+    {0x1.fd88da3d12526p-1, 0x1.917a6bc29b42cp-4},
+    {0x1.fe9cdad01883ap-1, 0x1.2d52092ce19f6p-4},
+    {0x1.ff621e3796d7ep-1, 0x1.91f65f10dd814p-5},
+    {0x1.ffd886084cd0dp-1, 0x1.92155f7a3667ep-6},
+    {0x1.0000000000000p+0, 0.0},
+    {0x1.ffd886084cd0dp-1, -0x1.92155f7a3667ep-6},
+    {0x1.ff621e3796d7ep-1, -0x1.91f65f10dd814p-5},
+    {0x1.fe9cdad01883ap-1, -0x1.2d52092ce19f6p-4},
+    {0x1.fd88da3d12526p-1, -0x1.917a6bc29b42cp-4},
+    {0x1.fc26470e19fd3p-1, -0x1.f564e56a9730ep-4},
+    {0x1.fa7557f08a517p-1, -0x1.2c8106e8e613ap-3},
+    {0x1.f8764fa714ba9p-1, -0x1.5e214448b3fc6p-3},
+    {0x1.f6297cff75cb0p-1, -0x1.8f8b83c69a60bp-3},
+    {0x1.f38f3ac64e589p-1, -0x1.c0b826a7e4f63p-3},
+    {0x1.f0a7efb9230d7p-1, -0x1.f19f97b215f1bp-3},
+    {0x1.ed740e7684963p-1, -0x1.111d262b1f677p-2},
+    {0x1.e9f4156c62ddap-1, -0x1.294062ed59f06p-2},
+    {0x1.e6288ec48e112p-1, -0x1.4135c94176601p-2},
+    {0x1.e212104f686e5p-1, -0x1.58f9a75ab1fddp-2},
+    {0x1.ddb13b6ccc23cp-1, -0x1.7088530fa459fp-2},
+    {0x1.d906bcf328d46p-1, -0x1.87de2a6aea963p-2},
+    {0x1.d4134d14dc93ap-1, -0x1.9ef7943a8ed8ap-2},
+    {0x1.ced7af43cc773p-1, -0x1.b5d1009e15cc0p-2},
+    {0x1.c954b213411f5p-1, -0x1.cc66e9931c45ep-2},
+    {0x1.c38b2f180bdb1p-1, -0x1.e2b5d3806f63bp-2},
+    {0x1.bd7c0ac6f952ap-1, -0x1.f8ba4dbf89abap-2},
+    {0x1.b728345196e3ep-1, -0x1.073879922ffeep-1},
+    {0x1.b090a58150200p-1, -0x1.11eb3541b4b23p-1},
+    {0x1.a9b66290ea1a3p-1, -0x1.1c73b39ae68c8p-1},
+    {0x1.a29a7a0462782p-1, -0x1.26d054cdd12dfp-1},
+    {0x1.9b3e047f38741p-1, -0x1.30ff7fce17035p-1},
+    {0x1.93a22499263fbp-1, -0x1.3affa292050b9p-1},
+    {0x1.8bc806b151741p-1, -0x1.44cf325091dd6p-1},
+    {0x1.83b0e0bff976ep-1, -0x1.4e6cabbe3e5e9p-1},
+    {0x1.7b5df226aafafp-1, -0x1.57d69348ceca0p-1},
+    {0x1.72d0837efff96p-1, -0x1.610b7551d2cdfp-1},
+    {0x1.6a09e667f3bcdp-1, -0x1.6a09e667f3bcdp-1},
+    {0x1.610b7551d2cdfp-1, -0x1.72d0837efff96p-1},
+    {0x1.57d69348ceca0p-1, -0x1.7b5df226aafafp-1},
+    {0x1.4e6cabbe3e5e9p-1, -0x1.83b0e0bff976ep-1},
+    {0x1.44cf325091dd6p-1, -0x1.8bc806b151741p-1},
+    {0x1.3affa292050b9p-1, -0x1.93a22499263fbp-1},
+    {0x1.30ff7fce17035p-1, -0x1.9b3e047f38741p-1},
+    {0x1.26d054cdd12dfp-1, -0x1.a29a7a0462782p-1},
+    {0x1.1c73b39ae68c8p-1, -0x1.a9b66290ea1a3p-1},
+    {0x1.11eb3541b4b23p-1, -0x1.b090a58150200p-1},
+    {0x1.073879922ffeep-1, -0x1.b728345196e3ep-1},
+    {0x1.f8ba4dbf89abap-2, -0x1.bd7c0ac6f952ap-1},
+    {0x1.e2b5d3806f63bp-2, -0x1.c38b2f180bdb1p-1},
+    {0x1.cc66e9931c45ep-2, -0x1.c954b213411f5p-1},
+    {0x1.b5d1009e15cc0p-2, -0x1.ced7af43cc773p-1},
+    {0x1.9ef7943a8ed8ap-2, -0x1.d4134d14dc93ap-1},
+    {0x1.87de2a6aea963p-2, -0x1.d906bcf328d46p-1},
+    {0x1.7088530fa459fp-2, -0x1.ddb13b6ccc23cp-1},
+    {0x1.58f9a75ab1fddp-2, -0x1.e212104f686e5p-1},
+    {0x1.4135c94176601p-2, -0x1.e6288ec48e112p-1},
+    {0x1.294062ed59f06p-2, -0x1.e9f4156c62ddap-1},
+    {0x1.111d262b1f677p-2, -0x1.ed740e7684963p-1},
+    {0x1.f19f97b215f1bp-3, -0x1.f0a7efb9230d7p-1},
+    {0x1.c0b826a7e4f63p-3, -0x1.f38f3ac64e589p-1},
+    {0x1.8f8b83c69a60bp-3, -0x1.f6297cff75cb0p-1},
+    {0x1.5e214448b3fc6p-3, -0x1.f8764fa714ba9p-1},
+    {0x1.2c8106e8e613ap-3, -0x1.fa7557f08a517p-1},
+    {0x1.f564e56a9730ep-4, -0x1.fc26470e19fd3p-1},
+    {0x1.917a6bc29b42cp-4, -0x1.fd88da3d12526p-1},
+    {0x1.2d52092ce19f6p-4, -0x1.fe9cdad01883ap-1},
+    {0x1.91f65f10dd814p-5, -0x1.ff621e3796d7ep-1},
+    {0x1.92155f7a3667ep-6, -0x1.ffd886084cd0dp-1},
+    {0.0, -0x1.0000000000000p+0},
+    {-0x1.92155f7a3667ep-6, -0x1.ffd886084cd0dp-1},
+    {-0x1.91f65f10dd814p-5, -0x1.ff621e3796d7ep-1},
+    {-0x1.2d52092ce19f6p-4, -0x1.fe9cdad01883ap-1},
+    {-0x1.917a6bc29b42cp-4, -0x1.fd88da3d12526p-1},
+    {-0x1.f564e56a9730ep-4, -0x1.fc26470e19fd3p-1},
+    {-0x1.2c8106e8e613ap-3, -0x1.fa7557f08a517p-1},
+    {-0x1.5e214448b3fc6p-3, -0x1.f8764fa714ba9p-1},
+    {-0x1.8f8b83c69a60bp-3, -0x1.f6297cff75cb0p-1},
+    {-0x1.c0b826a7e4f63p-3, -0x1.f38f3ac64e589p-1},
+    {-0x1.f19f97b215f1bp-3, -0x1.f0a7efb9230d7p-1},
+    {-0x1.111d262b1f677p-2, -0x1.ed740e7684963p-1},
+    {-0x1.294062ed59f06p-2, -0x1.e9f4156c62ddap-1},
+    {-0x1.4135c94176601p-2, -0x1.e6288ec48e112p-1},
+    {-0x1.58f9a75ab1fddp-2, -0x1.e212104f686e5p-1},
+    {-0x1.7088530fa459fp-2, -0x1.ddb13b6ccc23cp-1},
+    {-0x1.87de2a6aea963p-2, -0x1.d906bcf328d46p-1},
+    {-0x1.9ef7943a8ed8ap-2, -0x1.d4134d14dc93ap-1},
+    {-0x1.b5d1009e15cc0p-2, -0x1.ced7af43cc773p-1},
+    {-0x1.cc66e9931c45ep-2, -0x1.c954b213411f5p-1},
+    {-0x1.e2b5d3806f63bp-2, -0x1.c38b2f180bdb1p-1},
+    {-0x1.f8ba4dbf89abap-2, -0x1.bd7c0ac6f952ap-1},
+    {-0x1.073879922ffeep-1, -0x1.b728345196e3ep-1},
+    {-0x1.11eb3541b4b23p-1, -0x1.b090a58150200p-1},
+    {-0x1.1c73b39ae68c8p-1, -0x1.a9b66290ea1a3p-1},
+    {-0x1.26d054cdd12dfp-1, -0x1.a29a7a0462782p-1},
+    {-0x1.30ff7fce17035p-1, -0x1.9b3e047f38741p-1},
+    {-0x1.3affa292050b9p-1, -0x1.93a22499263fbp-1},
+    {-0x1.44cf325091dd6p-1, -0x1.8bc806b151741p-1},
+    {-0x1.4e6cabbe3e5e9p-1, -0x1.83b0e0bff976ep-1},
+    {-0x1.57d69348ceca0p-1, -0x1.7b5df226aafafp-1},
+    {-0x1.610b7551d2cdfp-1, -0x1.72d0837efff96p-1},
+    {-0x1.6a09e667f3bcdp-1, -0x1.6a09e667f3bcdp-1},
+    {-0x1.72d0837efff96p-1, -0x1.610b7551d2cdfp-1},
+    {-0x1.7b5df226aafafp-1, -0x1.57d69348ceca0p-1},
+    {-0x1.83b0e0bff976ep-1, -0x1.4e6cabbe3e5e9p-1},
+    {-0x1.8bc806b151741p-1, -0x1.44cf325091dd6p-1},
+    {-0x1.93a22499263fbp-1, -0x1.3affa292050b9p-1},
+    {-0x1.9b3e047f38741p-1, -0x1.30ff7fce17035p-1},
+    {-0x1.a29a7a0462782p-1, -0x1.26d054cdd12dfp-1},
+    {-0x1.a9b66290ea1a3p-1, -0x1.1c73b39ae68c8p-1},
+    {-0x1.b090a58150200p-1, -0x1.11eb3541b4b23p-1},
+    {-0x1.b728345196e3ep-1, -0x1.073879922ffeep-1},
+    {-0x1.bd7c0ac6f952ap-1, -0x1.f8ba4dbf89abap-2},
+    {-0x1.c38b2f180bdb1p-1, -0x1.e2b5d3806f63bp-2},
+    {-0x1.c954b213411f5p-1, -0x1.cc66e9931c45ep-2},
+    {-0x1.ced7af43cc773p-1, -0x1.b5d1009e15cc0p-2},
+    {-0x1.d4134d14dc93ap-1, -0x1.9ef7943a8ed8ap-2},
+    {-0x1.d906bcf328d46p-1, -0x1.87de2a6aea963p-2},
+    {-0x1.ddb13b6ccc23cp-1, -0x1.7088530fa459fp-2},
+    {-0x1.e212104f686e5p-1, -0x1.58f9a75ab1fddp-2},
+    {-0x1.e6288ec48e112p-1, -0x1.4135c94176601p-2},
+    {-0x1.e9f4156c62ddap-1, -0x1.294062ed59f06p-2},
+    {-0x1.ed740e7684963p-1, -0x1.111d262b1f677p-2},
+    {-0x1.f0a7efb9230d7p-1, -0x1.f19f97b215f1bp-3},
+    {-0x1.f38f3ac64e589p-1, -0x1.c0b826a7e4f63p-3},
+    {-0x1.f6297cff75cb0p-1, -0x1.8f8b83c69a60bp-3},
+    {-0x1.f8764fa714ba9p-1, -0x1.5e214448b3fc6p-3},
+    {-0x1.fa7557f08a517p-1, -0x1.2c8106e8e613ap-3},
+    {-0x1.fc26470e19fd3p-1, -0x1.f564e56a9730ep-4},
+    {-0x1.fd88da3d12526p-1, -0x1.917a6bc29b42cp-4},
+    {-0x1.fe9cdad01883ap-1, -0x1.2d52092ce19f6p-4},
+    {-0x1.ff621e3796d7ep-1, -0x1.91f65f10dd814p-5},
+    {-0x1.ffd886084cd0dp-1, -0x1.92155f7a3667ep-6},
+    {-0x1.0000000000000p+0, 0.0},
+    {-0x1.ffd886084cd0dp-1, 0x1.92155f7a3667ep-6},
+    {-0x1.ff621e3796d7ep-1, 0x1.91f65f10dd814p-5},
+    {-0x1.fe9cdad01883ap-1, 0x1.2d52092ce19f6p-4},
+    {-0x1.fd88da3d12526p-1, 0x1.917a6bc29b42cp-4},
+    {-0x1.fc26470e19fd3p-1, 0x1.f564e56a9730ep-4},
+    {-0x1.fa7557f08a517p-1, 0x1.2c8106e8e613ap-3},
+    {-0x1.f8764fa714ba9p-1, 0x1.5e214448b3fc6p-3},
+    {-0x1.f6297cff75cb0p-1, 0x1.8f8b83c69a60bp-3},
+    {-0x1.f38f3ac64e589p-1, 0x1.c0b826a7e4f63p-3},
+    {-0x1.f0a7efb9230d7p-1, 0x1.f19f97b215f1bp-3},
+    {-0x1.ed740e7684963p-1, 0x1.111d262b1f677p-2},
+    {-0x1.e9f4156c62ddap-1, 0x1.294062ed59f06p-2},
+    {-0x1.e6288ec48e112p-1, 0x1.4135c94176601p-2},
+    {-0x1.e212104f686e5p-1, 0x1.58f9a75ab1fddp-2},
+    {-0x1.ddb13b6ccc23cp-1, 0x1.7088530fa459fp-2},
+    {-0x1.d906bcf328d46p-1, 0x1.87de2a6aea963p-2},
+    {-0x1.d4134d14dc93ap-1, 0x1.9ef7943a8ed8ap-2},
+    {-0x1.ced7af43cc773p-1, 0x1.b5d1009e15cc0p-2},
+    {-0x1.c954b213411f5p-1, 0x1.cc66e9931c45ep-2},
+    {-0x1.c38b2f180bdb1p-1, 0x1.e2b5d3806f63bp-2},
+    {-0x1.bd7c0ac6f952ap-1, 0x1.f8ba4dbf89abap-2},
+    {-0x1.b728345196e3ep-1, 0x1.073879922ffeep-1},
+    {-0x1.b090a58150200p-1, 0x1.11eb3541b4b23p-1},
+    {-0x1.a9b66290ea1a3p-1, 0x1.1c73b39ae68c8p-1},
+    {-0x1.a29a7a0462782p-1, 0x1.26d054cdd12dfp-1},
+    {-0x1.9b3e047f38741p-1, 0x1.30ff7fce17035p-1},
+    {-0x1.93a22499263fbp-1, 0x1.3affa292050b9p-1},
+    {-0x1.8bc806b151741p-1, 0x1.44cf325091dd6p-1},
+    {-0x1.83b0e0bff976ep-1, 0x1.4e6cabbe3e5e9p-1},
+    {-0x1.7b5df226aafafp-1, 0x1.57d69348ceca0p-1},
+    {-0x1.72d0837efff96p-1, 0x1.610b7551d2cdfp-1},
+    {-0x1.6a09e667f3bcdp-1, 0x1.6a09e667f3bcdp-1},
+    {-0x1.610b7551d2cdfp-1, 0x1.72d0837efff96p-1},
+    {-0x1.57d69348ceca0p-1, 0x1.7b5df226aafafp-1},
+    {-0x1.4e6cabbe3e5e9p-1, 0x1.83b0e0bff976ep-1},
+    {-0x1.44cf325091dd6p-1, 0x1.8bc806b151741p-1},
+    {-0x1.3affa292050b9p-1, 0x1.93a22499263fbp-1},
+    {-0x1.30ff7fce17035p-1, 0x1.9b3e047f38741p-1},
+    {-0x1.26d054cdd12dfp-1, 0x1.a29a7a0462782p-1},
+    {-0x1.1c73b39ae68c8p-1, 0x1.a9b66290ea1a3p-1},
+    {-0x1.11eb3541b4b23p-1, 0x1.b090a58150200p-1},
+    {-0x1.073879922ffeep-1, 0x1.b728345196e3ep-1},
+    {-0x1.f8ba4dbf89abap-2, 0x1.bd7c0ac6f952ap-1},
+    {-0x1.e2b5d3806f63bp-2, 0x1.c38b2f180bdb1p-1},
+    {-0x1.cc66e9931c45ep-2, 0x1.c954b213411f5p-1},
+    {-0x1.b5d1009e15cc0p-2, 0x1.ced7af43cc773p-1},
+    {-0x1.9ef7943a8ed8ap-2, 0x1.d4134d14dc93ap-1},
+    {-0x1.87de2a6aea963p-2, 0x1.d906bcf328d46p-1},
+    {-0x1.7088530fa459fp-2, 0x1.ddb13b6ccc23cp-1},
+    {-0x1.58f9a75ab1fddp-2, 0x1.e212104f686e5p-1},
+    {-0x1.4135c94176601p-2, 0x1.e6288ec48e112p-1},
+    {-0x1.294062ed59f06p-2, 0x1.e9f4156c62ddap-1},
+    {-0x1.111d262b1f677p-2, 0x1.ed740e7684963p-1},
+    {-0x1.f19f97b215f1bp-3, 0x1.f0a7efb9230d7p-1},
+    {-0x1.c0b826a7e4f63p-3, 0x1.f38f3ac64e589p-1},
+    {-0x1.8f8b83c69a60bp-3, 0x1.f6297cff75cb0p-1},
+    {-0x1.5e214448b3fc6p-3, 0x1.f8764fa714ba9p-1},
+    {-0x1.2c8106e8e613ap-3, 0x1.fa7557f08a517p-1},
+    {-0x1.f564e56a9730ep-4, 0x1.fc26470e19fd3p-1},
+    {-0x1.917a6bc29b42cp-4, 0x1.fd88da3d12526p-1},
+    {-0x1.2d52092ce19f6p-4, 0x1.fe9cdad01883ap-1},
+    {-0x1.91f65f10dd814p-5, 0x1.ff621e3796d7ep-1},
+    {-0x1.92155f7a3667ep-6, 0x1.ffd886084cd0dp-1},
+};
+
 // sin x and cos x by table lookup: P. T. P. Tang, "Table-lookup algorithms for elementary
 // functions and their error analysis" (1991), with the three-part argument reduction of
 // W. J. Cody and W. Waite, "Software Manual for the Elementary Functions" (1980).
@@ -55,13 +317,16 @@ __device__ __forceinline__ double2 cexp2(double2 z) {
 //   sin x = S_k cos r + C_k sin r,   cos x = C_k cos r - S_k sin r,
 // with (S_k, C_k) = (sin, cos)(2pi k / 256) from the table and the Taylor series of sin r
 // to r^7 and of cos r to r^6 (the next terms are below 2e-20).  Absolute error about
-// 1.5e-16.  |x| > 2e4, and NaN, go to sincos().
+// 1.5e-16.  Near a zero of sin or cos (x close to a multiple of pi/2) the error is also
+// small relative to the result: the table holds exact zeros there and the reduction keeps
+// r to a few ulps of itself (a restatement of these steps in 60-digit arithmetic gives
+// 4e-16 relative for phases within 1e-9 of k pi).  |x| > 2e4, and NaN, go to sincos().
 constexpr double kScC1 = 0x1.921fb54400000p-6;
 constexpr double kScC2 = 0x1.0b4611a600000p-40;
 constexpr double kScC3 = 0x1.3198a2e037073p-75;
 constexpr double kScInv = 40.74366543152521;  // 256 / (2 pi)
 
-__device__ __forceinline__ void sincos_tab(double x, const double2* __restrict__ tab, double* s, double* c) {
+__device__ __forceinline__ void sincos_tab(double x, double* s, double* c) {
   if (!(fabs(x) <= 2.0e4)) {
     sincos(x, s, c);
     return;
@@ -70,16 +335,16 @@ __device__ __forceinline__ void sincos_tab(double x, const double2* __restrict__
   double r = fma(-kd, kScC1, x);
   r = fma(-kd, kScC2, r);
   r = fma(-kd, kScC3, r);
-  const double2 t = __ldg(tab + ((int)kd & 255));  // (S_k, C_k); k mod 256 in two's complement
+  const double2 t = __ldg(g_sincos_tab + ((int)kd & 255));  // (S_k, C_k); k mod 256 in two's complement
   const double r2 = r * r;
   const double sr = fma(r * r2, fma(r2, fma(r2, -1.0 / 5040.0, 1.0 / 120.0), -1.0 / 6.0), r);
   const double cr = fma(r2, fma(r2, fma(r2, -1.0 / 720.0, 1.0 / 24.0), -0.5), 1.0);
   *s = fma(t.x, cr, t.y * sr);
   *c = fma(t.y, cr, -(t.x * sr));
 }
-__device__ __forceinline__ double2 cexp_tab(double2 z, const double2* __restrict__ tab) {
+__device__ __forceinline__ double2 cexp_tab(double2 z) {
   double s, c;
-  sincos_tab(z.y, tab, &s, &c);
+  sincos_tab(z.y, &s, &c);
   if (z.x == 0.0) return make_double2(c, s);  // a pure phase (real pulse parameters)
   const double e = exp(z.x);
   return make_double2(e * c, e * s);
@@ -91,38 +356,6 @@ __device__ __forceinline__ double2 light_arg(double2 kx, double2 ky, double2 dx,
   return cadd(cmul(kx, dx), cmul(ky, dy));
 }
 
-// The (sin, cos)(2pi k / 256) table of the current device, made once on the host in long
-// double and rounded to double.
-const double2* sincos_table(int* status) {
-  static std::mutex mu;
-  static double2* tab[64] = {};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 64) {
-    *status = e != cudaSuccess ? check_cuda(e) : KPM_ERR_UNSUPPORTED;
-    return nullptr;
-  }
-  std::lock_guard<std::mutex> lock(mu);
-  if (!tab[dev]) {
-    double2 host[256];
-    const long double two_pi = 6.283185307179586476925286766559005768L;
-    for (int k = 0; k < 256; ++k) {
-      const long double a = two_pi * (long double)k / 256.0L;
-      host[k] = make_double2((double)sinl(a), (double)cosl(a));
-    }
-    double2* d = nullptr;
-    e = cudaMalloc(&d, sizeof(host));
-    if (e == cudaSuccess) e = cudaMemcpy(d, host, sizeof(host), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) {
-      if (d) cudaFree(d);
-      *status = check_cuda(e);
-      return nullptr;
-    }
-    tab[dev] = d;
-  }
-  *status = KPM_OK;
-  return tab[dev];
-}
 
 // cos(x + iy) = cos x cosh y - i sin x sinh y
 __device__ __forceinline__ double2 ccos2(double2 z) {
@@ -156,11 +389,10 @@ void light_coefficients(const double* params, double2* a, double2* kx, double2* 
 }
 
 __global__ void light_kernel(int64_t count, double2 a, double2 kx, double2 ky, const double2* __restrict__ data,
-                             const double2* __restrict__ dx, const double2* __restrict__ dy, double2* __restrict__ out,
-                             const double2* __restrict__ tab) {
+                             const double2* __restrict__ dx, const double2* __restrict__ dy, double2* __restrict__ out) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
     const double2 z = light_arg(kx, ky, dx[i], dy[i]);
-    out[i] = cmul(cmul(a, data[i]), cexp_tab(z, tab));
+    out[i] = cmul(cmul(a, data[i]), cexp_tab(z));
   }
 }
 
@@ -173,13 +405,12 @@ __global__ void light_kernel(int64_t count, double2 a, double2 kx, double2 ky, c
 // a2 = 2a: the stored values are 2H (doubling is exact, so 2a data e = 2 (a data e) bit for bit).
 __global__ void light_update_kernel(int64_t n, int64_t n_pad, int L, double2 a2, double2 kx, double2 ky,
                                     const double2* __restrict__ data, const double2* __restrict__ dx,
-                                    const double2* __restrict__ dy, double2* __restrict__ val,
-                                    const double2* __restrict__ tab) {
+                                    const double2* __restrict__ dy, double2* __restrict__ val) {
   for (int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; row < n; row += (int64_t)gridDim.x * blockDim.x) {
     for (int s = 0; s < L; ++s) {
       const int64_t k = row * L + s;
       const double2 z = light_arg(kx, ky, dx[k], dy[k]);
-      const double2 e = (z.x == 0.0 && z.y == 0.0) ? make_double2(1.0, 0.0) : cexp_tab(z, tab);
+      const double2 e = (z.x == 0.0 && z.y == 0.0) ? make_double2(1.0, 0.0) : cexp_tab(z);
       val[(int64_t)s * n_pad + row] = cmul(cmul(a2, data[k]), e);
     }
   }
@@ -236,14 +467,11 @@ int kpm_light_modifier(int64_t count, const double* params, const double* data, 
   if (count < 1 || !params || !data || !dx || !dy || !data_new) return KPM_ERR_INVALID_ARG;
   double2 a, kx, ky;
   light_coefficients(params, &a, &kx, &ky);
-  int st = KPM_OK;
-  const double2* tab = sincos_table(&st);
-  if (!tab) return st;
   cudaStream_t s = stream_of(stream);
   light_kernel<<<grid_for_count(count), 256, 0, s>>>(count, a, kx, ky, reinterpret_cast<const double2*>(data),
                                                      reinterpret_cast<const double2*>(dx),
                                                      reinterpret_cast<const double2*>(dy),
-                                                     reinterpret_cast<double2*>(data_new), tab);
+                                                     reinterpret_cast<double2*>(data_new));
   return check_cuda(cudaGetLastError());
 }
 
@@ -253,13 +481,10 @@ int kpm_ell_light_update(kpm_ell* h, const double* params, const double* data0, 
   if (h->is_real) return KPM_ERR_DTYPE;  // H(t) is complex: create the operator with KPM_FLAG_COMPLEX
   double2 a, kx, ky;
   light_coefficients(params, &a, &kx, &ky);
-  int st = KPM_OK;
-  const double2* tab = sincos_table(&st);
-  if (!tab) return st;
   cudaStream_t s = stream_of(stream);
   light_update_kernel<<<grid_for_count(h->n), 256, 0, s>>>(
       h->n, h->n_pad, h->L, make_double2(2.0 * a.x, 2.0 * a.y), kx, ky, reinterpret_cast<const double2*>(data0), reinterpret_cast<const double2*>(dx),
-      reinterpret_cast<const double2*>(dy), static_cast<double2*>(h->val64), tab);
+      reinterpret_cast<const double2*>(dy), static_cast<double2*>(h->val64));
   KPM_TRY(check_cuda(cudaGetLastError()));
   return values_changed(h, s);
 }

@@ -9,13 +9,24 @@
 // kpm_cheb_moments_noalloc reads the operator straight from the caller's
 // device arrays in jclsquant's padded row-major ELL layout and keeps its own
 // working vectors and moment partials in one file-scope device array of fixed
-// size, g_noalloc_scratch (kNoAllocScratchBytes, about 33 MiB).  Every GPU that
-// loads this library holds that array until the process exits.  The call
+// size, g_noalloc_scratch (kNoAllocScratchBytes, about 33 MiB).  The call
 // allocates nothing: no cudaMalloc, no cudaFree, no allocating library routine.
 //
-// Set-up: the first call on a device looks up the device address of the array
-// with cudaGetSymbolAddress while that device is current, once per device, and
-// caches it.  Make that first call on each device outside any stream capture.
+// When the array is reserved: with lazy module loading (CUDA_MODULE_LOADING=LAZY, the
+// default since CUDA 12.2) the library's device code, this array included, is loaded
+// into a CUDA context on the first use of the library in that context -- for a caller
+// that uses only this entry point, its first call there.  That first call can therefore
+// fail with KPM_ERR_CUDA when the context has no room left for the array, and it can
+// synchronise the device.  Make it at set-up time, while memory is available and
+// outside any stream capture, or set CUDA_MODULE_LOADING=EAGER so the array is reserved
+// when the context loads the library.  From then on the context holds the array until
+// it is destroyed or the process exits.
+//
+// Address: each call looks up the array's device address in the CUDA context that is
+// current on the calling thread (cudaGetSymbolAddress, which after the module load only
+// reads a table and allocates nothing).  A __device__ array has a different address in
+// every context, so a host application that makes its own driver-API context must have
+// that context current when it calls.
 //
 // Sharing: every call on a device uses the same array and leaves its contents
 // behind.  Each call writes every scratch word it later reads (vectors,
@@ -25,8 +36,6 @@
 // Serialise them.
 #include <cuda_runtime.h>
 #include <stdint.h>
-
-#include <mutex>
 
 #include "../../include/kpm.h"
 
@@ -43,28 +52,15 @@ constexpr size_t kNoAllocScratchBytes = 2 * kVecBytes + kPartBytes + 256;
 // Layout: [T_a : kNoAllocMaxRows double2][T_b : same][partials][status int]
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mutex;
-void* g_scratch_addr[kMaxDevices] = {nullptr};
-
-// Device address of the scratch array on the current device (looked up once).
-int scratch_for_current_device(char** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+// Device address of the scratch array in the calling thread's current CUDA context.
+int scratch_for_current_context(char** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
     (void)cudaGetLastError();
     return KPM_ERR_CUDA;
   }
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_addr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p) {
-      (void)cudaGetLastError();
-      return KPM_ERR_CUDA;
-    }
-    g_scratch_addr[dev] = p;
-  }
-  *out = static_cast<char*>(g_scratch_addr[dev]);
+  *out = static_cast<char*>(p);
   return KPM_OK;
 }
 
@@ -181,7 +177,7 @@ extern "C" int kpm_cheb_moments_noalloc(const double* data, const int32_t* indic
   if (!data || !indices || !v || !mu || len_row < 1 || n < 1 || M < 1) return KPM_ERR_INVALID_ARG;
   if (n > kNoAllocMaxRows) return KPM_ERR_TOO_LARGE;
   char* base = nullptr;
-  int rc = scratch_for_current_device(&base);
+  int rc = scratch_for_current_context(&base);
   if (rc != KPM_OK) return rc;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   double2* ta = reinterpret_cast<double2*>(base);

@@ -9,6 +9,8 @@ from __future__ import annotations
 
 import numpy as np
 
+from . import errors
+
 
 def _diagonal_add(A, diagonal_array):
     """data with diagonal_array[row] added to every valid (row, row) slot
@@ -56,8 +58,7 @@ def modifier_velocity(A, direction=None):
     """V = -i H o d  (d = dx_vec or dy_vec; jclsquant/modifiers.py:56-79)."""
     d = _direction_vec(A, direction)
     if d is None:
-        print(" You must introduce a valid direction: 0,1,2 or x,y,z ")
-        return None
+        return errors.missing(" You must introduce a valid direction: 0,1,2 or x,y,z ")
     return (-1j) * np.asarray(d, dtype=np.complex128) * np.asarray(A.data, dtype=np.complex128)
 
 
@@ -65,8 +66,7 @@ def modifier_velocity_bounds(A, direction=None):
     """H o d / a  (jclsquant/modifiers.py:82-105)."""
     d = _direction_vec(A, direction)
     if d is None:
-        print(" You must introduce a valid direction: 0,1,2 or x,y,z ")
-        return None
+        return errors.missing(" You must introduce a valid direction: 0,1,2 or x,y,z ")
     s = 1 / ((A.bounds[1] - A.bounds[0]) / 2) + 0j
     return s * np.asarray(d, dtype=np.complex128) * np.asarray(A.data, dtype=np.complex128)
 
@@ -75,8 +75,7 @@ def modifier_diagonal_anderson(A, W=None, seed=None):
     """Add Anderson disorder W*(2U - 1) on the diagonal, U from default_rng(seed)
     (jclsquant/modifiers.py:287-309)."""
     if W is None:
-        print("You must introduce a disorder strength to modify the system. ")
-        return None
+        return errors.missing("You must introduce a disorder strength to modify the system. ")
     rng = np.random.default_rng(seed)
     diag = W * (2 * rng.random(int(A.shape[0])) - 1)
     return _diagonal_add(A, diag)
@@ -87,8 +86,7 @@ def _light_params(modifier_id, modifier_params, t):
     """(a, A0, t, w, Tp, eta) of the light forms (jclsquant/modifiers.py:133-182, 369-413),
     or None after the reference's message."""
     if modifier_id is None or modifier_params is None:
-        print(' You must introduce a valid id : light, circle,light_packed or circle packed with irs valid parameters .')
-        return None
+        return errors.missing(' You must introduce a valid id : light, circle,light_packed or circle packed with irs valid parameters .')
     pol_eta = {"r": 1.0, "l": -1.0}
     if modifier_id == "linear":
         A0, w = modifier_params
@@ -96,8 +94,7 @@ def _light_params(modifier_id, modifier_params, t):
     if modifier_id == "circle":
         A0, w, pol = modifier_params
         if pol not in pol_eta:
-            print('You must introduce a valid polarization')
-            return None
+            return errors.missing('You must introduce a valid polarization')
         return (1.0, A0, t, w, 0.0, pol_eta[pol])
     if modifier_id == "linear_packed":
         A0, w, Tp = modifier_params
@@ -105,11 +102,9 @@ def _light_params(modifier_id, modifier_params, t):
     if modifier_id == "circle_packed":
         A0, w, pol, Tp = modifier_params
         if pol not in pol_eta:
-            print('You must introduce a valid polarization')
-            return None
+            return errors.missing('You must introduce a valid polarization')
         return (1.0, A0, t, w, Tp, pol_eta[pol])
-    print(' You must introduce a valid id : light, circle,light_packed or circle packed with irs valid parameters .')
-    return None
+    return errors.missing(' You must introduce a valid id : light, circle,light_packed or circle packed with irs valid parameters .')
 
 
 def _complex_params(values):
@@ -213,8 +208,7 @@ def modifier_hoppings_c_r(A, data_new, dx_vec_new, dy_vec_new, modifier_id=None,
         a0, b, Aq, wq, pol, S = modifier_params
         e_pol, q = _phonon_polarisation(pol, int(A.shape[0]), a0)
         if e_pol is None:
-            print('You must introduce a valid polarization')
-            return None
+            return errors.missing('You must introduce a valid polarization')
         S = np.asarray(S)
         dn, xn, yn = phonon_modifier_device(A.data, A.indices, A.dx_vec, A.dy_vec, A.len_row, a0, b, Aq, wq, t, q,
                                             e_pol[:, 0], e_pol[:, 1], S[:, 0], S[:, 1], data_new, dx_vec_new,

@@ -21,7 +21,7 @@ from oracle import oracle
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("case", ["irregular_300", "honeycomb_8x8", "complex_open_6x5"])
+@pytest.mark.parametrize("case", ["honeycomb_8x8", "complex_open_6x5", "ref_graphene_256", "irregular_300"])
 def test_withheld_stage_times_out_and_reports(cuda_lib, case):
     import torch
 
@@ -38,7 +38,12 @@ def test_withheld_stage_times_out_and_reports(cuda_lib, case):
         t0 = time.perf_counter()
         st = cuda_lib.kpm_ell_test_timeout(h, 20_000_000, None)
         dt = time.perf_counter() - t0
-        assert st == _capi.KPM_ERR_TIMEOUT, cuda_lib.kpm_strerror(st)
+        if case == "irregular_300":
+            # 9 complex slots per row: four shared-memory stages exceed the producer-warp
+            # kernel's limit, so the hook launches nothing and says so
+            assert st == _capi.KPM_ERR_UNSUPPORTED
+        else:
+            assert st == _capi.KPM_ERR_TIMEOUT, cuda_lib.kpm_strerror(st)
         assert dt < 5.0
         assert cuda_lib.kpm_ell_check(h, None) == _capi.KPM_OK  # read once, then cleared
         # the operator and the context are intact: moments as before

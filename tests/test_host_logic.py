@@ -149,3 +149,28 @@ def test_honeycomb_ensemble_is_seeded_and_rescaled():
         assert rows.max() <= 1 / 1.01 + 1e-12
     v = batched.ensemble_vectors([8, 18], 2, seed0=3)
     assert v.shape == (2, 26) and np.allclose(np.abs(v), 1.0)
+
+
+def test_strict_error_mode(capsys):
+    """Default: the reference's message and None.  Strict mode: ValueError with that message."""
+    from minijclsquant_gb300 import errors
+    from minijclsquant_gb300 import recurrence_functions as rf
+
+    H = _h8()
+    assert rf.rec_A_tab(8, H, None) is None
+    assert modifier_velocity(H, "w") is None
+    assert "You must introduce a vector." in capsys.readouterr().out
+    with errors.strict():
+        with pytest.raises(ValueError, match="introduce a vector"):
+            rf.rec_A_tab(8, H, None)
+        with pytest.raises(ValueError, match="valid direction"):
+            modifier_velocity(H, "w")
+        with pytest.raises(ValueError, match="velocity"):
+            rf.rec_com_A_vec(8, H, None, np.ones(8), np.ones(H.shape[0]))
+    assert not errors.is_strict()
+    errors.set_strict(True)
+    try:
+        with pytest.raises(ValueError):
+            rf.rec_A_vec(8, H, None, np.ones(H.shape[0]))
+    finally:
+        errors.set_strict(False)

@@ -79,6 +79,10 @@ def parse():
     ap.add_argument("--kubo-Nm", type=int, default=256)
     ap.add_argument("--kubo-R", type=int, default=4)
     ap.add_argument("--no-config1", action="store_true", help="skip the 8192-site DOS configuration")
+    ap.add_argument("--no-adjoint-kubo", action="store_true", help="skip the differentiable conductivity")
+    ap.add_argument("--adjk-cells", type=int, default=512)
+    ap.add_argument("--adjk-Nm", type=int, default=256)
+    ap.add_argument("--adjk-fd", type=int, default=8, help="parameters checked by central differences")
     ap.add_argument("--e2e-max-steps", type=int, default=6, help="host-pointer passes timed for e2e")
     return ap.parse_args()
 
@@ -852,6 +856,91 @@ def run_adjoint(a, steps, warmup):
                          "stencil4_h1e-4": {"params": min(16, len(params)), "max_abs_err_over_max_grad": worst4}}}
 
 
+def run_adjoint_kubo(a, steps):
+    """The differentiable Kubo-Greenwood conductivity: honeycomb cells x cells, learnable FP64
+    on-site potentials U[-0.5, 0.5] eV and per-bond hoppings -2.7 + U[-0.1, 0.1] eV, V_x =
+    -i H o dx, Nm moments, R = 4 vectors, sigma(E) on 64 energies in [-0.9 a, 0.9 a], loss = L2
+    against sigma of another disorder draw.  Everything complex128; the moment matrix and the
+    two mixing products of the backward are cuBLAS FP64 GEMMs.  Reports forward and
+    forward+backward times (their ratio is the adjoint cost) and central differences
+    (h = 1e-6) on a few seeded parameters."""
+    import torch
+
+    from minijclsquant_gb300 import adjoint
+
+    cells, Nm, R = a.adjk_cells, a.adjk_Nm, 4
+    n = 2 * cells * cells
+    rng = np.random.default_rng(21)
+    on0 = rng.uniform(-0.5, 0.5, n)
+    hop0 = -2.7 + rng.uniform(-0.1, 0.1, 3 * cells * cells)
+    t0 = time.perf_counter()
+    plan = adjoint.KuboPlan(cells, cells, Nm, R=R, n_energies=64, onsite0=on0, hopping0=hop0)
+    setup_s = time.perf_counter() - t0
+    rng_t = np.random.default_rng(22)
+    with torch.no_grad():
+        target = adjoint.kpm_sigma(torch.tensor(rng_t.uniform(-0.5, 0.5, n), device="cuda"),
+                                   torch.tensor(-2.7 + rng_t.uniform(-0.1, 0.1, plan.n_bonds), device="cuda"), plan)
+    onsite = torch.tensor(on0, dtype=torch.float64, device="cuda", requires_grad=True)
+    hop = torch.tensor(hop0, dtype=torch.float64, device="cuda", requires_grad=True)
+
+    def fwd():
+        with torch.no_grad():
+            return adjoint.sigma_l2_loss(onsite, hop, plan, target)
+
+    def fwd_bwd():
+        onsite.grad = None
+        hop.grad = None
+        loss = adjoint.sigma_l2_loss(onsite, hop, plan, target)
+        loss.backward()
+        return loss
+
+    def timeit(fn, k):
+        fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / k
+
+    k = max(1, min(steps, 3))
+    torch.cuda.reset_peak_memory_stats()
+    t_f = timeit(fwd, k)
+    t_fb = timeit(fwd_bwd, k)
+    peak_gb = torch.cuda.max_memory_allocated() / 1e9
+    go, gh = onsite.grad.detach().cpu().numpy(), hop.grad.detach().cpu().numpy()
+    scale = max(np.max(np.abs(go)), np.max(np.abs(gh)))
+    pick = np.random.default_rng(23)
+    half = a.adjk_fd // 2
+    params = [("onsite", int(i)) for i in pick.choice(n, half, replace=False)] + \
+             [("hopping", int(i)) for i in pick.choice(plan.n_bonds, a.adjk_fd - half, replace=False)]
+    h = 1e-6
+    worst = 0.0
+    with torch.no_grad():
+        for which, i in params:
+            p = onsite if which == "onsite" else hop
+            old = p[i].item()
+            p[i] = old + h
+            lp = fwd().item()
+            p[i] = old - h
+            lm = fwd().item()
+            p[i] = old
+            an = (go if which == "onsite" else gh)[i]
+            worst = max(worst, abs(an - (lp - lm) / (2 * h)) / scale)
+    gemm_flops = 8.0 * Nm * Nm * n * R  # the forward's moment-matrix GEMM (complex MACs x 8)
+    del plan
+    torch.cuda.empty_cache()
+    return {"workload": "differentiable Kubo-Greenwood sigma_xx(E): honeycomb %dx%d cells (%d sites), learnable on-site "
+                        "and per-bond hoppings, V_x = -i H o dx, Nm=%d, R=%d, 64 energies, L2 loss against another "
+                        "disorder draw" % (cells, cells, n, Nm, R),
+            "forward_ms": 1e3 * t_f, "forward_backward_ms": 1e3 * t_fb, "fwd_plus_bwd_over_fwd": t_fb / t_f,
+            "steps": k, "setup_s": setup_s, "peak_device_gb": peak_gb,
+            "forward_gemm_fp64_tflops": gemm_flops / t_f / 1e12,
+            "fd_check": {"params": len(params), "h": h, "max_abs_err_over_max_grad": worst},
+            "note": "complex128 throughout; tables of every order per vector (the moment matrix couples all "
+                    "orders), cuBLAS FP64 GEMMs for mu_nm and the backward's C T products"}
+
+
 def _fp64_mu_block(Hd, Vd, idx, L, v, sel):
     """FP64 mu[n][m] = <v| V T_n(H) V T_m(H) |v> for n, m in `sel`, from plain torch gathers
     on the device (complex128 ELL products): L_n = T_n(H) V v, R_m = V T_m(H) v."""
@@ -1321,6 +1410,9 @@ def run_ours(a):
     if not a.no_kubo:
         torch.cuda.empty_cache()
         line["kubo"] = run_kubo(a, peaks, a.steps, a.warmup)
+    if not a.no_adjoint_kubo:
+        torch.cuda.empty_cache()
+        line["adjoint_kubo"] = run_adjoint_kubo(a, a.steps)
     if not a.no_config1:
         torch.cuda.empty_cache()
         line["config1_dos"] = run_config1(a, world)

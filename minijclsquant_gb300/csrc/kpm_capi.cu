@@ -836,8 +836,10 @@ int kpm_ell_destroy(kpm_ell* h) {
   if (h->err_flag) cudaFree(h->err_flag);
   Workspace& w = h->ws;
   DevBuf* bufs[] = {&w.ta, &w.tb, &w.tc, &w.td, &w.vl, &w.vr, &w.acc, &w.acc2, &w.part, &w.coef,
-                    &w.ckpt, &w.seg, &w.grad};
+                    &w.ckpt, &w.seg, &w.grad, &w.red, &w.vf, &w.gin, &w.gin2, &w.gout};
   for (DevBuf* b : bufs) release(*b);
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  h->graphs.clear();
   kpm_ell_profile(h, 0);
   delete h;
   return KPM_OK;
@@ -921,6 +923,99 @@ int kpm_ell_dot(kpm_ell* h, double a_re, double a_im, double b_re, double b_im, 
   return KPM_OK;
 }
 
+// Operators whose working set sits in L2 run a recursion of short step launches; there the
+// launch latency, not memory, sets the pace.  Such a group's recursion is recorded once into
+// a CUDA graph (per shape and buffer set) and replayed as one launch: the caller's vectors
+// are copied into staging buffers first and the moments copied out after, so the recorded
+// pointers never change.  KPM_NO_GRAPH in the environment turns this off.
+static bool small_recursion(const kpm_ell_s* h, int Rg, int M) {
+  return (int64_t)h->n_pad * Rg <= ((int64_t)1 << 20) && M >= 16 && !h->prof && !getenv("KPM_NO_GRAPH");
+}
+
+static int moments_group_graph(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const double* v_r,
+                               const double* v_l, double* mu, double* mu_rr, cudaStream_t s) {
+  const int sets = mu_rr ? 2 : 1;
+  StepConfig cfg;
+  KPM_TRY(step_config(h, f32, Rg, sets, s, &cfg));  // tuned (and cached) before anything is recorded
+  const bool ffm = M > 2 && cfg.kind == 2 && ff_moment_products(f32, sets);
+  const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
+  const size_t nb = (size_t)h->n * Rg * sizeof(double2);
+  const size_t mb = (size_t)Rg * M * sizeof(double2);
+  Workspace& ws = h->ws;
+  // everything the recursion touches is sized now: nothing may allocate while it is recorded
+  KPM_TRY(ensure(ws.ta, vb));
+  KPM_TRY(ensure(ws.tb, vb));
+  KPM_TRY(ensure(ws.vl, vb));
+  if (sets == 2) KPM_TRY(ensure(ws.vr, vb));
+  KPM_TRY(ensure(ws.part, (size_t)kChunk * sets * cfg.grid * Rg * sizeof(double2)));
+  if (ffm) KPM_TRY(ensure(ws.vf, (size_t)h->n_pad * Rg * sizeof(float4)));
+  KPM_TRY(ensure(ws.gin, nb));
+  if (v_l) KPM_TRY(ensure(ws.gin2, nb));
+  KPM_TRY(ensure(ws.gout, sets * mb));
+  double* in_r = static_cast<double*>(ws.gin.p);
+  double* in_l = v_l ? static_cast<double*>(ws.gin2.p) : nullptr;
+  double* out = static_cast<double*>(ws.gout.p);
+  double* out2 = sets == 2 ? out + 2 * (size_t)Rg * M : nullptr;
+  const void* bufs[10] = {ws.ta.p, ws.tb.p, ws.vl.p, sets == 2 ? ws.vr.p : nullptr, ws.part.p,
+                          ffm ? ws.vf.p : nullptr, in_r, in_l, out, f32 ? h->val32 : h->val64};
+  cudaGraphExec_t exec = nullptr;
+  for (size_t i = 0; i < h->graphs.size(); ++i) {
+    MomentGraph& g = h->graphs[i];
+    if (g.f32 == (int)f32 && g.Rg == Rg && g.M == M && g.sets == sets && g.has_vl == (v_l != nullptr) &&
+        g.ffm == (int)ffm && g.kind == cfg.kind && g.U == cfg.U && g.grid == cfg.grid) {
+      if (std::equal(bufs, bufs + 10, g.bufs)) {
+        exec = g.exec;
+      } else {
+        cudaGraphExecDestroy(g.exec);
+        h->graphs.erase(h->graphs.begin() + i);
+      }
+      break;
+    }
+  }
+  // the group's vectors (rows r0 .. r0 + Rg - 1 of [R][n], contiguous) into the staging buffers
+  KPM_CUDA_TRY(cudaMemcpyAsync(in_r, v_r + 2 * (size_t)r0 * h->n, nb, cudaMemcpyDeviceToDevice, s));
+  if (v_l) KPM_CUDA_TRY(cudaMemcpyAsync(in_l, v_l + 2 * (size_t)r0 * h->n, nb, cudaMemcpyDeviceToDevice, s));
+  if (!exec) {
+    cudaStream_t cs;
+    KPM_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph;
+    cudaError_t eb = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (eb != cudaSuccess) {
+      cudaStreamDestroy(cs);
+      KPM_CUDA_TRY(eb);
+    }
+    const int rc = moments_group(h, f32, Rg, 0, Rg, M, in_r, in_l, out, out2, cs);
+    const cudaError_t ec = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (rc != KPM_OK) {
+      if (ec == cudaSuccess) cudaGraphDestroy(graph);
+      return rc;
+    }
+    KPM_CUDA_TRY(ec);
+    const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    KPM_CUDA_TRY(ei);
+    MomentGraph g;
+    g.f32 = (int)f32;
+    g.Rg = Rg;
+    g.M = M;
+    g.sets = sets;
+    g.has_vl = v_l != nullptr;
+    g.ffm = (int)ffm;
+    g.kind = cfg.kind;
+    g.U = cfg.U;
+    g.grid = cfg.grid;
+    std::copy(bufs, bufs + 10, g.bufs);
+    g.exec = exec;
+    h->graphs.push_back(g);
+  }
+  KPM_CUDA_TRY(cudaGraphLaunch(exec, s));
+  // moments of rows r0 .. r0 + Rg - 1 of [R][M]
+  KPM_CUDA_TRY(cudaMemcpyAsync(mu + 2 * (size_t)r0 * M, out, mb, cudaMemcpyDeviceToDevice, s));
+  if (mu_rr) KPM_CUDA_TRY(cudaMemcpyAsync(mu_rr + 2 * (size_t)r0 * M, out2, mb, cudaMemcpyDeviceToDevice, s));
+  return KPM_OK;
+}
+
 int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r, const double* v_l, double* mu,
                      double* mu_rr, void* stream) {
   if (!h || !v_r || !mu || R < 1 || M < 1) return KPM_ERR_INVALID_ARG;
@@ -939,7 +1034,10 @@ int kpm_cheb_moments(kpm_ell* h, int dtype, int R, int M, const double* v_r, con
   if (f32) KPM_TRY(ensure_f32_values(h, s));
   for (int r0 = 0; r0 < R;) {
     const int Rg = pow2_group(R - r0);
-    KPM_TRY(moments_group(h, f32, R, r0, Rg, M, v_r, v_l, mu, mu_rr, s));
+    if (small_recursion(h, Rg, M) && !(!v_l && !mu_rr && use_doubling(h, M)))
+      KPM_TRY(moments_group_graph(h, f32, R, r0, Rg, M, v_r, v_l, mu, mu_rr, s));
+    else
+      KPM_TRY(moments_group(h, f32, R, r0, Rg, M, v_r, v_l, mu, mu_rr, s));
     r0 += Rg;
   }
   return KPM_OK;

@@ -76,6 +76,15 @@ struct Workspace {
   DevBuf ckpt, seg, grad;  // adjoint: checkpoint pairs, recomputed segment, per-slot gradient
   DevBuf red;              // doubling: reduced sets [2][R][K + 1], then the per-vector corrections
   DevBuf vf;               // float-pair left vectors of the FP64 recursion's moment products
+  DevBuf gin, gin2, gout;  // graph replays of small recursions: staged inputs and moments
+};
+
+// A recorded moment recursion of one vector group (L2-resident operators replay it as one
+// CUDA graph launch): its shape and every device pointer it was recorded with.
+struct MomentGraph {
+  int f32 = 0, Rg = 0, M = 0, sets = 0, has_vl = 0, ffm = 0, kind = 0, U = 0, grid = 0;
+  const void* bufs[10] = {};
+  cudaGraphExec_t exec = nullptr;
 };
 
 // Kernel choice for the recursion step of one (precision, R group, moment sets).
@@ -119,6 +128,8 @@ struct kpm_ell_s {
   uint64_t same_cols_id = 0;
   // fingerprint of the column structure (sum of (column - row) * (2 slot + 1))
   uint64_t structure = 0;
+  // recorded recursions of small operators (kpm_cheb_moments)
+  std::vector<kpm::MomentGraph> graphs;
 };
 
 namespace kpm {

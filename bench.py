@@ -1284,7 +1284,8 @@ def run_ours(a):
     _capi.check(lib.kpm_ell_step_config(op.handle, _capi.dtype_code(a.dtype), R, ctypes.byref(kind), ctypes.byref(rpt),
                                         ctypes.byref(grid), ctypes.byref(us)))
     kname = {1: "cheb_next_staged_kernel (bulk-copy staged, %d row(s)/thread)" % rpt.value,
-             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value}.get(
+             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value,
+             3: "cheb_next_ws_kernel (bulk-copy staged, producer warp, 1 row/thread, four CTAs per SM)"}.get(
         kind.value, "cheb_step_kernel (grid-stride, MODE_NEXT STORE|MOM1)")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
@@ -1295,7 +1296,7 @@ def run_ours(a):
     # FP64 FMAs per site-step: the recursion's 2L (real values) or 4L, plus the moment's 4 unless
     # the producer-warp kernel forms the moment products in float-float arithmetic (the default
     # for one moment set; KPM_MOMENTS_FP64=1 turns it off)
-    ff_products = (a.dtype == "c128" and not doubled and kind.value == 2
+    ff_products = (a.dtype == "c128" and not doubled and kind.value in (2, 3)
                    and os.environ.get("KPM_MOMENTS_FP64", "") in ("", "0"))
     rec_fma = 2 * L if op.is_real else 4 * L
     fma_per_site_step = rec_fma + (6 if doubled else (0 if ff_products else 4))

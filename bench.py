@@ -750,6 +750,12 @@ def run_batched(a, hbm_peak, steps, warmup):
             "moment_error_vs_c128": {"max_rel_mu0": float(per_order.max()),
                                      "by_order": {str(m): float(per_order[m]) for m in (1, 10, 100, 500, M - 1) if m < M}},
             "setup_s": setup_s, "graph": "one CUDA graph launch per recursion",
+            "graph_vs_step_sum": {
+                "step_kernel_us": cfg64["step_us"], "step_launches": executed_steps(M, doubled),
+                "steps_sum_ms": executed_steps(M, doubled) * cfg64["step_us"] * 1e-3, "graph_ms": ms64,
+                "other_ms_frac": (ms64 - executed_steps(M, doubled) * cfg64["step_us"] * 1e-3) / ms64,
+                "note": "time of the graph replay not spent in the step kernel (first step, reductions, launch "
+                        "gaps): the most a single persistent launch could save"},
             "step_kernel": {"c64": cfg64, "c128": cfg128},
             "gpu_launches_per_step": 1 + executed_steps(M, doubled) + (M + 127) // 128 + (3 if doubled else 0)}
 

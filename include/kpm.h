@@ -456,6 +456,11 @@ int kpm_ell_test_timeout(kpm_ell* h, int64_t budget_cycles, void* stream);
 int kpm_ell_profile(kpm_ell* h, int enable);
 int kpm_ell_profile_read(kpm_ell* h, double* loop_ms, int64_t* step_launches, int64_t* rows_per_launch);
 int kpm_measure_fp64_fma_rate(double* fma_per_second, void* stream);
+/* kpm_mu_gemm_path: which kernel the last tensor-core contraction (kpm_mu_nm,
+ * kpm_mu_contract) ran: 1 = operands brought in by the TMA engine (mu_gemm_tma_kernel),
+ * 0 = operands loaded by the threads (mu_gemm_kernel; KPM_MU_GEMM=legacy forces it),
+ * -1 = none yet. */
+int kpm_mu_gemm_path(void);
 
 #ifdef __cplusplus
 }

@@ -97,6 +97,7 @@ SIGNATURES = {
     "kpm_ell_profile": (_I, [_P, _I]),
     "kpm_ell_profile_read": (_I, [_P, ctypes.POINTER(_D), ctypes.POINTER(_I64), ctypes.POINTER(_I64)]),
     "kpm_measure_fp64_fma_rate": (_I, [ctypes.POINTER(_D), _P]),
+    "kpm_mu_gemm_path": (_I, []),
 }
 
 _lock = threading.Lock()

@@ -20,9 +20,13 @@
 // The reference has no such contraction (its conductivity is the time-domain
 // correlator of kpm_time_sigma); the operator conventions are those of
 // modifier_velocity (jclsquant/modifiers.py:56-79).
+#include <cuda.h>  // CUtensorMap and its enums; the encoder is looked up at run time (no libcuda link)
+
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 #include "kpm_async.cuh"
 #include "kpm_internal.cuh"
@@ -280,6 +284,265 @@ __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmPara
   if (warp == 0) tmem_dealloc(tmem, kTmemCols);
 }
 
+// ---- the same contraction with its operand tiles brought in by the TMA engine -----------
+// mu_gemm_kernel's threads load every K tile from global memory themselves (two tiles
+// ahead in registers) and meet at a CTA barrier per tile, so the loop waits on those loads.
+// Here one thread issues cp.async.bulk.tensor copies kRawStages tiles ahead into a ring of
+// raw stages, and the threads only split a tile that has landed.  The 4-D tensor map
+// (4 floats x 8 rows x K chunks of 16 bytes x 8-row groups; strides 4 B, one row, 16 B,
+// 8 rows) makes each copy land in the MMA's canonical no-swizzle K-major layout (core
+// matrices of 8 rows x 16 bytes, LBO 128 B, SBO 512 B), so a thread reads its raw chunk and
+// writes its hi / lo / swapped chunks at the same offsets, free of bank conflicts.
+// Accumulation, chains, folds and partials are those of mu_gemm_kernel.
+constexpr int kRawStages = 4;
+constexpr uint32_t kRawBytes = 2 * kTileA;                    // raw A and B tiles, 16 KB
+constexpr uint32_t kTmaSmem = kRawStages * kRawBytes + kGemmStages * kStageBytes;  // 208 KB
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+      "%5}], [%6];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__global__ void __launch_bounds__(kGemmThreads, 1)
+    mu_gemm_tma_kernel(const GemmParams p, const __grid_constant__ CUtensorMap map_a,
+                       const __grid_constant__ CUtensorMap map_b) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  __shared__ __align__(8) uint64_t bars[kGemmStages];
+  __shared__ __align__(8) uint64_t rawbar[kRawStages];
+  __shared__ __align__(8) uint64_t accbar[2];
+  __shared__ uint32_t tmem_slot;
+
+  const int tile = blockIdx.x;
+  const int n0 = (tile / p.mt) * kTile, m0 = (tile % p.mt) * kTile;
+  const int64_t k_begin = (int64_t)blockIdx.y * p.k_per_cta;
+  const int64_t k_end = min(p.K, k_begin + p.k_per_cta);
+  const int k_tiles = k_end > k_begin ? (int)((k_end - k_begin) / kKt) : 0;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int q = warp & 3;
+  const int cb = (warp >> 2) * kColsPerThread;
+  const int half = cb / kTile;
+  const int row = 32 * q + lane;
+  const int64_t obase = (((int64_t)blockIdx.y * gridDim.x + tile) * 2 + half) * kTileElems +
+                        (int64_t)(cb % kTile) * kTile + row;
+  float* ohi = p.part_hi + obase;
+  float* olo = p.part_lo + obase;
+
+  if (k_tiles == 0) {
+    for (int c = 0; c < kColsPerThread; ++c) {
+      ohi[c * kTile] = 0.f;
+      olo[c * kTile] = 0.f;
+    }
+    return;
+  }
+  unsigned char* raw = smem;                                  // kRawStages x [A raw | B raw]
+  unsigned char* split = smem + kRawStages * kRawBytes;       // kGemmStages x [Ahi Alo BXhi BXlo]
+  if (tid == 0) {
+    for (int s = 0; s < kGemmStages; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < kRawStages; ++s) mbar_init(&rawbar[s], 1);
+    mbar_init(&accbar[0], 1);
+    mbar_init(&accbar[1], 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&tmem_slot, kTmemCols);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t split_base = static_cast<uint32_t>(__cvta_generic_to_shared(split));
+  const uint32_t idesc = idesc_tf32(kTile, 2 * kTile);
+  // raw tile t: A rows n0.., B rows m0.., K floats k_begin + 16 t ..
+  const int kc0 = (int)(k_begin / 4);
+  auto issue_raw = [&](int t) {
+    const int rs = t % kRawStages;
+    mbar_arrive_expect_tx(&rawbar[rs], kRawBytes);
+    tma_load_4d(raw + (size_t)rs * kRawBytes, &map_a, 0, 0, kc0 + t * (kKt / 4), n0 / 8, &rawbar[rs]);
+    tma_load_4d(raw + (size_t)rs * kRawBytes + kTileA, &map_b, 0, 0, kc0 + t * (kKt / 4), m0 / 8, &rawbar[rs]);
+  };
+  int raw_issued = 0;  // thread 0: raw tiles whose copies were issued
+  if (tid == 0) {
+    for (; raw_issued < kRawStages && raw_issued < k_tiles; ++raw_issued) issue_raw(raw_issued);
+  }
+
+  float run[kColsPerThread];
+#pragma unroll
+  for (int i = 0; i < kColsPerThread; ++i) run[i] = 0.f;
+  bool first_flush = true;
+  int chains_in_l1 = 0;
+
+  auto fold_chain = [&](int c) -> bool {
+    bool ok = mbar_wait_bounded(&accbar[c & 1], (uint32_t)((c >> 1) & 1));
+    ok = __all_sync(0xffffffffu, ok);
+    if (!ok) return false;
+    tc_fence_after();
+    const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((c & 1) * 256 + cb);
+#pragma unroll
+    for (int g = 0; g < kColsPerThread / 16; ++g) {
+      float v[16];
+      tmem_ld16(base + (uint32_t)(g * 16), v);
+#pragma unroll
+      for (int i = 0; i < 16; ++i) run[g * 16 + i] = __fadd_rn(run[g * 16 + i], v[i]);
+    }
+    return true;
+  };
+  auto flush_l2 = [&]() {
+#pragma unroll
+    for (int c = 0; c < kColsPerThread; ++c) {
+      if (first_flush) {
+        ohi[c * kTile] = run[c];
+        olo[c * kTile] = 0.f;
+      } else {
+        const float a = ohi[c * kTile], b = run[c];
+        const float s = __fadd_rn(a, b);
+        const float bp = __fsub_rn(s, a);
+        const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
+        ohi[c * kTile] = s;
+        olo[c * kTile] = __fadd_rn(olo[c * kTile], e);
+      }
+      run[c] = 0.f;
+    }
+    first_flush = false;
+  };
+
+  const int crow = chunk_row(tid), ckc = chunk_kc(tid);
+  const uint32_t off = chunk_off(crow, ckc);
+  const uint32_t offs = chunk_off(kTile + crow, ckc);
+  int issued = 0;  // K tiles whose MMAs thread 0 has issued
+  int t = 0;
+  bool ok = true;
+  for (; t < k_tiles && ok; ++t) {
+    const int st = t % kGemmStages;
+    const int rs = t % kRawStages;
+    const int c = t / kChainTiles;
+    bool good = true;
+    if (t % kChainTiles == 0 && c >= 2) {
+      good = fold_chain(c - 2);
+      if (good && ++chains_in_l1 == kLevel1Chains) {
+        flush_l2();
+        chains_in_l1 = 0;
+      }
+    }
+    if (good && t >= kGemmStages)
+      good = mbar_wait_bounded(&bars[st], (uint32_t)(((t - kGemmStages) / kGemmStages) & 1));
+    if (good) good = mbar_wait_bounded(&rawbar[rs], (uint32_t)((t / kRawStages) & 1));
+    if (good) {
+      const unsigned char* rw = raw + (size_t)rs * kRawBytes;
+      unsigned char* stage = split + (size_t)st * kStageBytes;
+      {
+        const float4 x = *reinterpret_cast<const float4*>(rw + off);
+        const float4 hi = tf32x4(x);
+        const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
+        *reinterpret_cast<float4*>(stage + off) = hi;
+        *reinterpret_cast<float4*>(stage + kTileA + off) = lo;
+      }
+      {
+        const float4 x = *reinterpret_cast<const float4*>(rw + kTileA + off);
+        const float4 hi = tf32x4(x);
+        const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
+        unsigned char* bx = stage + 2 * kTileA;
+        *reinterpret_cast<float4*>(bx + off) = hi;
+        *reinterpret_cast<float4*>(bx + kTileBX + off) = lo;
+        *reinterpret_cast<float4*>(bx + offs) = make_float4(hi.y, -hi.x, hi.w, -hi.z);
+        *reinterpret_cast<float4*>(bx + kTileBX + offs) = make_float4(lo.y, -lo.x, lo.w, -lo.z);
+      }
+    }
+    fence_proxy_async_shared();
+    tc_fence_before();
+    if (__syncthreads_or(!good)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t s0 = split_base + (uint32_t)st * kStageBytes;
+      const uint32_t d = tmem + (uint32_t)((c & 1) * 256);
+#pragma unroll
+      for (int j = 0; j < kKt / 8; ++j) {
+        const uint32_t kofs = (uint32_t)j * 2 * kLBO;
+        const uint64_t a_hi = smem_desc(s0 + kofs, kLBO, kSBO);
+        const uint64_t a_lo = smem_desc(s0 + kTileA + kofs, kLBO, kSBO);
+        const uint64_t bx_hi = smem_desc(s0 + 2 * kTileA + kofs, kLBO, kSBO);
+        const uint64_t bx_lo = smem_desc(s0 + 2 * kTileA + kTileBX + kofs, kLBO, kSBO);
+        mma_tf32(d, a_hi, bx_hi, idesc, (t % kChainTiles) != 0 || j > 0);
+        mma_tf32(d, a_hi, bx_lo, idesc, true);
+        mma_tf32(d, a_lo, bx_hi, idesc, true);
+      }
+      mma_commit(&bars[st]);
+      if ((t + 1) % kChainTiles == 0 || t + 1 == k_tiles) mma_commit(&accbar[c & 1]);
+      issued = t + 1;
+      // every thread has read raw stage rs (the barrier above): refill it with tile t + kRawStages
+      if (raw_issued < k_tiles) {
+        fence_proxy_async_shared();
+        issue_raw(raw_issued);
+        ++raw_issued;
+      }
+    }
+  }
+  if (ok) {
+    const int nchains = (k_tiles + kChainTiles - 1) / kChainTiles;
+    bool good = true;
+    for (int c = max(0, nchains - 2); c < nchains && good; ++c) good = fold_chain(c);
+    ok = !__syncthreads_or(!good);
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicExch(p.err, KPM_ERR_TIMEOUT);
+      if (issued > 0)
+        (void)mbar_wait_bounded(&bars[(issued - 1) % kGemmStages], (uint32_t)(((issued - 1) / kGemmStages) & 1));
+      // raw copies issued but not yet read: wait (bounded) for them to land before the CTA leaves
+      for (int r = t; r < raw_issued; ++r) (void)mbar_wait_bounded(&rawbar[r % kRawStages], (uint32_t)((r / kRawStages) & 1));
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+    return;
+  }
+  flush_l2();
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tmem_dealloc(tmem, kTmemCols);
+}
+
+// cuTensorMapEncodeTiled from the driver, looked up once (nullptr if unavailable).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = []() -> EncodeTiledFn {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// The operand map of a [rows][lda] float matrix (rows a multiple of 128): dims (4 floats, 8 rows,
+// lda / 4 chunks, rows / 8 groups), box (4, 8, kKt / 4, 16) = one 128-row x 16-float tile in the
+// canonical layout.
+static bool operand_map(CUtensorMap* m, const float* base, int64_t lda, int rows) {
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[4] = {4, 8, (cuuint64_t)(lda / 4), (cuuint64_t)(rows / 8)};
+  const cuuint64_t strides[3] = {(cuuint64_t)lda * 4, 16, (cuuint64_t)lda * 4 * 8};
+  const cuuint32_t box[4] = {4, 8, (cuuint32_t)(kKt / 4), (cuuint32_t)(kTile / 8)};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // mu[n][m] = (accumulate ? mu : 0) + scale * sum_ks (hi + lo), Re and Im, in FP64.
 __global__ void mu_reduce_kernel(const float* __restrict__ hi, const float* __restrict__ lo, int KS, int tiles,
                                  int mt, int Nm, double scale, int accumulate, double2* __restrict__ mu) {
@@ -316,6 +579,9 @@ int contract_splits(int64_t K, int sm_count, int tiles) {
 // Floats of the partial buffer (hi and lo planes).
 size_t contract_part_floats(int KS, int tiles) { return (size_t)2 * KS * tiles * 2 * kTileElems; }
 
+// 1 when the last contraction ran mu_gemm_tma_kernel, 0 for mu_gemm_kernel (kpm_mu_gemm_path)
+static int g_last_gemm_tma = -1;
+
 int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, double scale, int accumulate,
                 double2* mu, float* part, int KS, int* err, cudaStream_t s) {
   static bool attr = false;
@@ -336,7 +602,23 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
   g.part_hi = part;
   g.part_lo = part + (size_t)KS * tiles * 2 * kTileElems;
   g.err = err;
-  mu_gemm_kernel<<<dim3(tiles, KS), kGemmThreads, kGemmSmem, s>>>(g);
+  // operands through the TMA engine when the tensor maps can be made (16-byte aligned rows,
+  // the driver's encoder present); KPM_MU_GEMM=legacy keeps the thread-loaded kernel
+  const char* force = getenv("KPM_MU_GEMM");
+  CUtensorMap ma, mb;
+  const bool tma = !(force && std::string(force) == "legacy") && operand_map(&ma, A, lda, mt * kTile) &&
+                   operand_map(&mb, B, lda, mt * kTile);
+  g_last_gemm_tma = tma ? 1 : 0;
+  if (tma) {
+    static bool attr_tma = false;
+    if (!attr_tma) {
+      KPM_CUDA_TRY(cudaFuncSetAttribute(mu_gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem));
+      attr_tma = true;
+    }
+    mu_gemm_tma_kernel<<<dim3(tiles, KS), kGemmThreads, kTmaSmem, s>>>(g, ma, mb);
+  } else {
+    mu_gemm_kernel<<<dim3(tiles, KS), kGemmThreads, kGemmSmem, s>>>(g);
+  }
   KPM_CUDA_TRY(cudaGetLastError());
   mu_reduce_kernel<<<(Nm * Nm + 255) / 256, 256, 0, s>>>(g.part_hi, g.part_lo, KS, tiles, mt, Nm, scale, accumulate,
                                                          mu);
@@ -349,6 +631,8 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
 using namespace kpm;
 
 extern "C" {
+
+int kpm_mu_gemm_path(void) { return g_last_gemm_tma; }
 
 int kpm_mu_contract(const float* L, const float* R, int64_t k_floats, int64_t ld, int Nm, double scale,
                     int accumulate, double* mu, void* stream) {

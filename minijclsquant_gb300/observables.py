@@ -9,6 +9,8 @@ grid).  With R random vectors ([R, N]) the DOS is the average over vectors.
 """
 from __future__ import annotations
 
+import functools
+
 import numpy as np
 
 from . import recurrence_functions as rf
@@ -34,6 +36,18 @@ def rescaled_energies(Ef_vec, bounds):
     return Ef_vec / a - (0.5 * (bounds[1] + bounds[0])) / a
 
 
+@functools.lru_cache(maxsize=16)
+def _dos_table(b0, b1, M, n_energies):
+    """(energies, the Jackson-damped delta moments [n_E, M]) of a grid, kept for reuse: the
+    table depends only on the bounds, M and the grid, not on the moments."""
+    bounds = (b0, b1)
+    Ef_vec = energy_grid(bounds, M, n_energies)
+    table = moments_delta_table(rescaled_energies(Ef_vec, bounds), M) * JacksonKernel(M)[None, :]
+    Ef_vec.setflags(write=False)
+    table.setflags(write=False)
+    return Ef_vec, table
+
+
 def dos_from_moments(mu, bounds, M, n_energies=None):
     """[E, rho(E)] with rho = Re sum_m delta_m(E~) g_m mu_m (jclsquant/observables.py:49-52).
 
@@ -43,11 +57,13 @@ def dos_from_moments(mu, bounds, M, n_energies=None):
     mu = np.asarray(mu)
     if mu.ndim == 2:
         mu = mu.mean(axis=0)
-    Ef_vec = energy_grid(bounds, M, n_energies)
-    table = moments_delta_table(rescaled_energies(Ef_vec, bounds), M) * JacksonKernel(M)[None, :]
+    Ef_vec, table = _dos_table(float(bounds[0]), float(bounds[1]), int(M),
+                               None if n_energies is None else int(n_energies))
     out = np.zeros((len(Ef_vec), 2))
     out[:, 0] = Ef_vec
-    out[:, 1] = np.real(table.astype(np.complex128) @ mu.astype(np.complex128))
+    # Re(table . mu) with a real table: two real products, no complex copy of the table
+    mu = mu.astype(np.complex128)
+    out[:, 1] = table @ mu.real
     return out
 
 

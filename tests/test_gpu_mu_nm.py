@@ -155,3 +155,24 @@ def test_fused_velocity_step_matches_separate_products(cuda_lib, monkeypatch, R)
     monkeypatch.delenv("KPM_MU_NM_UNFUSED", raising=False)
     assert cuda_lib.kpm_mu_nm(hop.handle, vop.handle, R, Nm, vs.data_ptr(), mu.data_ptr(), None) == 0
     assert np.max(np.abs(mu.cpu().numpy() - separate)) <= 1e-5 * np.max(np.abs(separate))
+
+
+@pytest.mark.parametrize("nvec,Nm", [(8, 256), (4096, 64), (70000, 200), (300001, 256)])
+def test_tma_contraction_equals_thread_loaded_kernel(cuda_lib, monkeypatch, nvec, Nm):
+    """The contraction whose operand tiles come in through the TMA engine (mu_gemm_tma_kernel)
+    runs by default, and its moment matrix equals, bit for bit, that of the kernel whose
+    threads load the operands (KPM_MU_GEMM=legacy): the same MMAs in the same order."""
+    rng = np.random.default_rng(nvec + Nm)
+    L = rng.normal(size=(256, 2 * nvec)).astype(np.float32)
+    Rm = rng.normal(size=(256, 2 * nvec)).astype(np.float32)
+    mu_tma = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
+    assert cuda_lib.kpm_mu_gemm_path() == 1
+    monkeypatch.setenv("KPM_MU_GEMM", "legacy")
+    mu_old = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
+    assert cuda_lib.kpm_mu_gemm_path() == 0
+    monkeypatch.delenv("KPM_MU_GEMM")
+    assert np.array_equal(mu_tma, mu_old)
+    Lc = L[:Nm, 0::2].astype(np.float64) + 1j * L[:Nm, 1::2]
+    Rc = Rm[:Nm, 0::2].astype(np.float64) + 1j * Rm[:Nm, 1::2]
+    ref = np.conj(Lc) @ Rc.T
+    assert np.max(np.abs(mu_tma - ref)) / np.max(np.abs(ref)) < 2e-5

@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--no-adjoint-kubo", action="store_true", help="skip the differentiable conductivity")
     ap.add_argument("--adjk-cells", type=int, default=512)
     ap.add_argument("--adjk-Nm", type=int, default=256)
-    ap.add_argument("--adjk-fd", type=int, default=6, help="parameters checked by central differences")
+    ap.add_argument("--adjk-fd", type=int, default=4, help="parameters checked by central differences")
     ap.add_argument("--e2e-max-steps", type=int, default=6, help="host-pointer passes timed for e2e")
     return ap.parse_args()
 
@@ -631,9 +631,9 @@ def run_reference_arm(a):
             "ms_per_step": 1e3 * tot / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic", "impl": "reference",
             "config": {"workload": "plain c128 KPM moments on the %d-site honeycomb operator of the GPU arm "
-                                   "(2048x2048 cells, W=%g eV, ELL width 4); sampled at M=%d moments and R=1 "
+                                   "(%dx%d cells, W=%g eV, ELL width 4); sampled at M=%d moments and R=1 "
                                    "vector per step (the GPU arm runs M=%d, R=%d; the unit, site-steps/s, is "
-                                   "per site, vector and order)" % (prob["n"], a.W, M, a.M, a.R),
+                                   "per site, vector and order)" % (prob["n"], a.cells, a.cells, a.W, M, a.M, a.R),
                        "sites": prob["n"], "M": M, "R": 1, "gpu_arm_M": a.M, "gpu_arm_R": a.R},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind, "sample": sample,
                              "cpu_model": cpu_model()},
@@ -909,7 +909,7 @@ def run_adjoint_kubo(a, steps):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / k
 
-    k = max(1, min(steps, 3))
+    k = max(1, min(steps, 2))
     torch.cuda.reset_peak_memory_stats()
     t_f = timeit(fwd, k)
     t_fb = timeit(fwd_bwd, k)
@@ -1290,8 +1290,7 @@ def run_ours(a):
     _capi.check(lib.kpm_ell_step_config(op.handle, _capi.dtype_code(a.dtype), R, ctypes.byref(kind), ctypes.byref(rpt),
                                         ctypes.byref(grid), ctypes.byref(us)))
     kname = {1: "cheb_next_staged_kernel (bulk-copy staged, %d row(s)/thread)" % rpt.value,
-             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value,
-             3: "cheb_next_ws_kernel (bulk-copy staged, producer warp, 1 row/thread, four CTAs per SM)"}.get(
+             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value}.get(
         kind.value, "cheb_step_kernel (grid-stride, MODE_NEXT STORE|MOM1)")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
@@ -1302,7 +1301,7 @@ def run_ours(a):
     # FP64 FMAs per site-step: the recursion's 2L (real values) or 4L, plus the moment's 4 unless
     # the producer-warp kernel forms the moment products in float-float arithmetic (the default
     # for one moment set; KPM_MOMENTS_FP64=1 turns it off)
-    ff_products = (a.dtype == "c128" and not doubled and kind.value in (2, 3)
+    ff_products = (a.dtype == "c128" and not doubled and kind.value == 2
                    and os.environ.get("KPM_MOMENTS_FP64", "") in ("", "0"))
     rec_fma = 2 * L if op.is_real else 4 * L
     fma_per_site_step = rec_fma + (6 if doubled else (0 if ff_products else 4))

@@ -96,12 +96,10 @@ int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M);
  * device (KPM_ERR_TIMEOUT if a bounded wait ran out), then clear it. */
 int kpm_ell_check(kpm_ell* h, void* stream);
 /* The recursion-step kernel chosen for (dtype, R): kind 0 = grid-stride,
- * 1 = bulk-copy staged, 2 = bulk-copy staged with a producer warp, 3 = the same
- * producer-warp step with float-float moment products compiled for four CTAs per
- * SM (complex128, real values, one moment set); rows per thread per tile; CTAs;
- * measured us per step.  A choice is timed once per operator shape and column
- * structure in a process and shared by later handles
- * (KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2|ws1dense forces one and bypasses that).
+ * 1 = bulk-copy staged, 2 = bulk-copy staged with a producer warp; rows per
+ * thread per tile; CTAs; measured us per step.  A choice is timed once per
+ * operator shape and column structure in a process and shared by later handles
+ * (KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2 forces one and bypasses that).
  * Operators of at most 2^20 / R padded rows (L2-resident recursions, where launch
  * latency sets the pace) replay each recursion of kpm_cheb_moments as one CUDA graph
  * launch, recorded on first use per shape (KPM_NO_GRAPH=1 launches step by step). */
@@ -457,9 +455,11 @@ int kpm_ell_profile(kpm_ell* h, int enable);
 int kpm_ell_profile_read(kpm_ell* h, double* loop_ms, int64_t* step_launches, int64_t* rows_per_launch);
 int kpm_measure_fp64_fma_rate(double* fma_per_second, void* stream);
 /* kpm_mu_gemm_path: which kernel the last tensor-core contraction (kpm_mu_nm,
- * kpm_mu_contract) ran: 1 = operands brought in by the TMA engine (mu_gemm_tma_kernel),
- * 0 = operands loaded by the threads (mu_gemm_kernel; KPM_MU_GEMM=legacy forces it),
- * -1 = none yet. */
+ * kpm_mu_contract) ran: bit 0 = operand tiles brought in by the TMA engine
+ * (mu_gemm_tma_kernel) rather than loaded by the threads (mu_gemm_kernel); bit 1 = the
+ * 64-byte-swizzled shared-memory operand layout rather than the no-swizzle one; -1 =
+ * none yet.  KPM_MU_GEMM=legacy|tma|legacy_plain|tma_plain picks one (default: legacy,
+ * swizzled). */
 int kpm_mu_gemm_path(void);
 
 #ifdef __cplusplus

@@ -111,7 +111,6 @@ int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepPar
     return f32 ? launch_staged_f32(real, R, cfg.U, p, cfg.grid, s) : launch_staged_f64(real, R, cfg.U, p, cfg.grid, s);
   if (cfg.kind == 2)
     return f32 ? launch_ws_f32(real, R, cfg.U, p, cfg.grid, s) : launch_ws_f64(real, R, cfg.U, p, cfg.grid, s);
-  if (cfg.kind == 3) return launch_ws_f64_dense(R, p, cfg.grid, s);
   return launch_step(f32, real, R, MODE_NEXT, EPI_STORE | (series ? EPI_SERIES : EPI_MOM1), p, cfg.grid, s);
 }
 
@@ -193,18 +192,6 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
       c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
       cands.push_back(c);
     }
-  // the float-float-products step at four CTAs per SM (FP64, real values, one set)
-  if (ffm && h->is_real && (f.empty() || f == "ws1dense")) {
-    const int occ = ws_ctas_f64_dense(Rg, h->L);
-    if (occ > 0) {
-      const int64_t ntiles = h->n_pad / staged_tile_rows(false, Rg, 1);
-      StepConfig c;
-      c.kind = 3;
-      c.U = 1;
-      c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
-      cands.push_back(c);
-    }
-  }
   if (cands.empty()) {  // a forced staged kernel that cannot serve this call (two moment sets)
     StepConfig c;
     c.kind = 0;
@@ -629,7 +616,7 @@ int moments_group(kpm_ell_s* h, bool f32, int R, int r0, int Rg, int M, const do
   p.tout = ws.tb.p;
   p.part = part;
   KPM_TRY(launch_step(f32, h->is_real, Rg, MODE_FIRST, EPI_STORE | EPI_MOM1, p, grid, s));
-  if (M > 2 && (cfg.kind == 2 || cfg.kind == 3) && ff_moment_products(f32, sets)) {
+  if (M > 2 && cfg.kind == 2 && ff_moment_products(f32, sets)) {
     // later steps: FP64 recursion, moment products in float-float arithmetic
     KPM_TRY(ensure(ws.vf, (size_t)h->n_pad * Rg * sizeof(float4)));
     KPM_TRY(pack_left_ff(v_l ? v_l : v_r, h->n, h->n_pad, R, r0, Rg, ws.vf.p, s));
@@ -950,7 +937,7 @@ static int moments_group_graph(kpm_ell_s* h, bool f32, int R, int r0, int Rg, in
   const int sets = mu_rr ? 2 : 1;
   StepConfig cfg;
   KPM_TRY(step_config(h, f32, Rg, sets, s, &cfg));  // tuned (and cached) before anything is recorded
-  const bool ffm = M > 2 && (cfg.kind == 2 || cfg.kind == 3) && ff_moment_products(f32, sets);
+  const bool ffm = M > 2 && cfg.kind == 2 && ff_moment_products(f32, sets);
   const size_t vb = (size_t)h->n_pad * Rg * (f32 ? sizeof(float2) : sizeof(double2));
   const size_t nb = (size_t)h->n * Rg * sizeof(double2);
   const size_t mb = (size_t)Rg * M * sizeof(double2);

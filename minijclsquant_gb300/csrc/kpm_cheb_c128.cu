@@ -39,25 +39,5 @@ int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff) {
   return Ws<double>::ctas_per_sm(real, R, U, L, nvec, ff);
 }
 
-int launch_ws_f64_dense(int R, const StepParams& p, int grid, cudaStream_t s) {
-  if (!p.vl_ff || !p.vl || p.dbl || p.series) return KPM_ERR_UNSUPPORTED;
-  switch (R) {
-    case 1: return launch_ws_dense<true, 1>(p, grid, s);
-    case 2: return launch_ws_dense<true, 2>(p, grid, s);
-    case 4: return launch_ws_dense<true, 4>(p, grid, s);
-    case 8: return launch_ws_dense<true, 8>(p, grid, s);
-    default: return KPM_ERR_UNSUPPORTED;
-  }
-}
-
-int ws_ctas_f64_dense(int R, int L) {
-  switch (R) {
-    case 1: return ws_ctas_per_sm_k<double, true, 1, 1, 1, kWsFF, 4>(L, 2);
-    case 2: return ws_ctas_per_sm_k<double, true, 2, 1, 1, kWsFF, 4>(L, 2);
-    case 4: return ws_ctas_per_sm_k<double, true, 4, 1, 1, kWsFF, 4>(L, 2);
-    case 8: return ws_ctas_per_sm_k<double, true, 8, 1, 1, kWsFF, 4>(L, 2);
-    default: return 0;
-  }
-}
 
 }  // namespace kpm

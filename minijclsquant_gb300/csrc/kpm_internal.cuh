@@ -89,8 +89,7 @@ struct MomentGraph {
 
 // Kernel choice for the recursion step of one (precision, R group, moment sets).
 struct StepConfig {
-  int kind = 0;  // 0: grid-stride kernel, 1: bulk-copy staged kernel, 2: staged with a producer warp,
-                 // 3: the producer-warp float-float-products step at four CTAs per SM (FP64, real)
+  int kind = 0;  // 0: grid-stride kernel, 1: bulk-copy staged kernel, 2: staged with a producer warp
   int U = 1;     // rows per thread per tile (staged)
   int grid = 0;  // CTAs
   float us = 0;  // measured time of one step launch when tuned
@@ -195,10 +194,6 @@ int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaSt
 int launch_ws_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
 // ff: CTAs of the float-float-products variant (one moment set, FP64 recursion)
 int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff = false);
-// The float-float-products FP64 step of a real operator (one row per thread) compiled for
-// four CTAs per SM (kpm_ws.cuh, launch_ws_dense): StepConfig kind 3.
-int launch_ws_f64_dense(int R, const StepParams& p, int grid, cudaStream_t s);
-int ws_ctas_f64_dense(int R, int L);
 int ws_ctas_f32(bool real, int R, int U, int L, int nvec);
 // Driver helpers (kpm_capi.cu).
 int pow2_group(int remaining);

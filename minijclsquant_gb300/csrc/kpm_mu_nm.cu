@@ -68,6 +68,28 @@ __device__ __forceinline__ uint32_t chunk_off(int r, int kc) {
   return (uint32_t)(r >> 3) * kSBO + (uint32_t)kc * kLBO + (uint32_t)(r & 7) * 16;
 }
 
+// Operand layouts of a 16-float K tile.  SW = false: the canonical no-swizzle K-major layout
+// above (core matrices of 8 rows x 16 B, LBO 128 B, SBO 512 B); the tensor core fetches the
+// 8-row groups of one MMA at 512-byte strides, all on the same shared-memory banks.
+// SW = true: the 64-byte-swizzled K-major layout: row r is 64 contiguous bytes at r * 64 with
+// its 16-byte chunk kc stored at chunk kc ^ ((r >> 1) & 3) (address bits [4,6) XOR bits
+// [7,9), the pattern repeating every 512 bytes = 8 rows), SBO 512 B; the chunks an MMA
+// fetches then spread over all banks.  The K = 8 step j of an MMA starts 32 j bytes in.
+template <bool SW>
+__device__ __forceinline__ uint32_t tile_off(int r, int kc) {
+  if constexpr (SW) return (uint32_t)r * 64u + ((uint32_t)(kc ^ ((r >> 1) & 3)) << 4);
+  return chunk_off(r, kc);
+}
+template <bool SW>
+__device__ __forceinline__ uint64_t operand_desc(uint32_t saddr) {
+  if constexpr (SW) return smem_desc(saddr, 16, 512) | ((uint64_t)4 << 61);  // swizzle mode 4: 64 B
+  return smem_desc(saddr, kLBO, kSBO);
+}
+template <bool SW>
+__device__ __forceinline__ uint32_t kstep_off(int j) {
+  return SW ? (uint32_t)j * 32u : (uint32_t)j * 2u * kLBO;
+}
+
 // The 16-byte chunk a thread moves: chunk c (0..511) of a 128-row x 16-float tile
 // is row ((c >> 5) << 3 | (c & 7)), k-chunk ((c >> 3) & 3), so the eight threads of
 // a shared-memory store phase write one 128-byte core-matrix column (no bank
@@ -87,6 +109,7 @@ __device__ __forceinline__ float4 tf32x4(float4 x) {
 // kColsPerThread columns), and every kLevel1Chains chains those sums go into a float-float
 // (hi, lo) partial in global memory.  The tensor core's FP32 accumulation thus
 // never runs longer than 3 * 2 * kChainTiles MMAs.
+template <bool SW>
 __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmParams p) {
   extern __shared__ __align__(1024) unsigned char smem[];
   __shared__ __align__(8) uint64_t bars[kGemmStages];
@@ -182,8 +205,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmPara
     float4 a, b;
   };
   const int crow = chunk_row(tid), ckc = chunk_kc(tid);
-  const uint32_t off = chunk_off(crow, ckc);
-  const uint32_t offs = chunk_off(kTile + crow, ckc);
+  const uint32_t off = tile_off<SW>(crow, ckc);
+  const uint32_t offs = tile_off<SW>(kTile + crow, ckc);
   const float* pa = p.A + (int64_t)(n0 + crow) * p.lda + k_begin + 4 * ckc;
   const float* pb = p.B + (int64_t)(m0 + crow) * p.lda + k_begin + 4 * ckc;
   auto load_tile = [&](int t, RawTile& r) {
@@ -236,11 +259,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmPara
       const uint32_t d = tmem + (uint32_t)((c & 1) * 256);
 #pragma unroll
       for (int j = 0; j < kKt / 8; ++j) {
-        const uint32_t kofs = (uint32_t)j * 2 * kLBO;
-        const uint64_t a_hi = smem_desc(s0 + kofs, kLBO, kSBO);
-        const uint64_t a_lo = smem_desc(s0 + kTileA + kofs, kLBO, kSBO);
-        const uint64_t bx_hi = smem_desc(s0 + 2 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t bx_lo = smem_desc(s0 + 2 * kTileA + kTileBX + kofs, kLBO, kSBO);
+        const uint32_t kofs = kstep_off<SW>(j);
+        const uint64_t a_hi = operand_desc<SW>(s0 + kofs);
+        const uint64_t a_lo = operand_desc<SW>(s0 + kTileA + kofs);
+        const uint64_t bx_hi = operand_desc<SW>(s0 + 2 * kTileA + kofs);
+        const uint64_t bx_lo = operand_desc<SW>(s0 + 2 * kTileA + kTileBX + kofs);
         mma_tf32(d, a_hi, bx_hi, idesc, (t % kChainTiles) != 0 || j > 0);
         mma_tf32(d, a_hi, bx_lo, idesc, true);
         mma_tf32(d, a_lo, bx_hi, idesc, true);
@@ -298,6 +321,13 @@ constexpr int kRawStages = 4;
 constexpr uint32_t kRawBytes = 2 * kTileA;                    // raw A and B tiles, 16 KB
 constexpr uint32_t kTmaSmem = kRawStages * kRawBytes + kGemmStages * kStageBytes;  // 208 KB
 
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int c0, int c1, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(smem_addr(bar))
+      : "memory");
+}
 __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
                                             uint64_t* bar) {
   asm volatile(
@@ -307,6 +337,7 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
       : "memory");
 }
 
+template <bool SW>
 __global__ void __launch_bounds__(kGemmThreads, 1)
     mu_gemm_tma_kernel(const GemmParams p, const __grid_constant__ CUtensorMap map_a,
                        const __grid_constant__ CUtensorMap map_b) {
@@ -363,8 +394,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   auto issue_raw = [&](int t) {
     const int rs = t % kRawStages;
     mbar_arrive_expect_tx(&rawbar[rs], kRawBytes);
-    tma_load_4d(raw + (size_t)rs * kRawBytes, &map_a, 0, 0, kc0 + t * (kKt / 4), n0 / 8, &rawbar[rs]);
-    tma_load_4d(raw + (size_t)rs * kRawBytes + kTileA, &map_b, 0, 0, kc0 + t * (kKt / 4), m0 / 8, &rawbar[rs]);
+    if constexpr (SW) {
+      tma_load_2d(raw + (size_t)rs * kRawBytes, &map_a, 4 * kc0 + t * kKt, n0, &rawbar[rs]);
+      tma_load_2d(raw + (size_t)rs * kRawBytes + kTileA, &map_b, 4 * kc0 + t * kKt, m0, &rawbar[rs]);
+    } else {
+      tma_load_4d(raw + (size_t)rs * kRawBytes, &map_a, 0, 0, kc0 + t * (kKt / 4), n0 / 8, &rawbar[rs]);
+      tma_load_4d(raw + (size_t)rs * kRawBytes + kTileA, &map_b, 0, 0, kc0 + t * (kKt / 4), m0 / 8, &rawbar[rs]);
+    }
   };
   int raw_issued = 0;  // thread 0: raw tiles whose copies were issued
   if (tid == 0) {
@@ -412,8 +448,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   };
 
   const int crow = chunk_row(tid), ckc = chunk_kc(tid);
-  const uint32_t off = chunk_off(crow, ckc);
-  const uint32_t offs = chunk_off(kTile + crow, ckc);
+  const uint32_t off = tile_off<SW>(crow, ckc);
+  const uint32_t offs = tile_off<SW>(kTile + crow, ckc);
   int issued = 0;  // K tiles whose MMAs thread 0 has issued
   int t = 0;
   bool ok = true;
@@ -465,11 +501,11 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
       const uint32_t d = tmem + (uint32_t)((c & 1) * 256);
 #pragma unroll
       for (int j = 0; j < kKt / 8; ++j) {
-        const uint32_t kofs = (uint32_t)j * 2 * kLBO;
-        const uint64_t a_hi = smem_desc(s0 + kofs, kLBO, kSBO);
-        const uint64_t a_lo = smem_desc(s0 + kTileA + kofs, kLBO, kSBO);
-        const uint64_t bx_hi = smem_desc(s0 + 2 * kTileA + kofs, kLBO, kSBO);
-        const uint64_t bx_lo = smem_desc(s0 + 2 * kTileA + kTileBX + kofs, kLBO, kSBO);
+        const uint32_t kofs = kstep_off<SW>(j);
+        const uint64_t a_hi = operand_desc<SW>(s0 + kofs);
+        const uint64_t a_lo = operand_desc<SW>(s0 + kTileA + kofs);
+        const uint64_t bx_hi = operand_desc<SW>(s0 + 2 * kTileA + kofs);
+        const uint64_t bx_lo = operand_desc<SW>(s0 + 2 * kTileA + kTileBX + kofs);
         mma_tf32(d, a_hi, bx_hi, idesc, (t % kChainTiles) != 0 || j > 0);
         mma_tf32(d, a_hi, bx_lo, idesc, true);
         mma_tf32(d, a_lo, bx_hi, idesc, true);
@@ -528,6 +564,20 @@ static EncodeTiledFn encode_tiled() {
   return fn;
 }
 
+// The 64-byte-swizzled operand map of a [rows][lda] float matrix: dims (lda floats, rows), box
+// (16 floats, 128 rows): one K tile lands as 128 rows of 64 bytes in the swizzled layout.
+static bool operand_map_sw(CUtensorMap* m, const float* base, int64_t lda, int rows) {
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)lda, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)lda * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)kKt, (cuuint32_t)kTile};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // The operand map of a [rows][lda] float matrix (rows a multiple of 128): dims (4 floats, 8 rows,
 // lda / 4 chunks, rows / 8 groups), box (4, 8, kKt / 4, 16) = one 128-row x 16-float tile in the
 // canonical layout.
@@ -579,16 +629,11 @@ int contract_splits(int64_t K, int sm_count, int tiles) {
 // Floats of the partial buffer (hi and lo planes).
 size_t contract_part_floats(int KS, int tiles) { return (size_t)2 * KS * tiles * 2 * kTileElems; }
 
-// 1 when the last contraction ran mu_gemm_tma_kernel, 0 for mu_gemm_kernel (kpm_mu_gemm_path)
+// the last contraction's kernel (kpm_mu_gemm_path): bit 0 TMA loads, bit 1 swizzled layout
 static int g_last_gemm_tma = -1;
 
 int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, double scale, int accumulate,
                 double2* mu, float* part, int KS, int* err, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    KPM_CUDA_TRY(cudaFuncSetAttribute(mu_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGemmSmem));
-    attr = true;
-  }
   const int mt = (Nm + kTile - 1) / kTile;
   const int tiles = mt * mt;
   GemmParams g;
@@ -602,23 +647,35 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
   g.part_hi = part;
   g.part_lo = part + (size_t)KS * tiles * 2 * kTileElems;
   g.err = err;
-  // operands through the TMA engine when the tensor maps can be made (16-byte aligned rows,
-  // the driver's encoder present); KPM_MU_GEMM=legacy keeps the thread-loaded kernel
+  // kernel: operand tiles loaded by the threads ("legacy") or by the TMA engine ("tma"), in the
+  // 64-byte-swizzled layout or the no-swizzle one ("_plain"); KPM_MU_GEMM picks one, the default
+  // is the threads' loads into the swizzled layout
   const char* force = getenv("KPM_MU_GEMM");
+  const std::string f = force ? force : "";
+  const bool want_tma = f == "tma" || f == "tma_plain";
+  const bool sw = !(f == "legacy_plain" || f == "tma_plain");
   CUtensorMap ma, mb;
-  const bool tma = !(force && std::string(force) == "legacy") && operand_map(&ma, A, lda, mt * kTile) &&
-                   operand_map(&mb, B, lda, mt * kTile);
-  g_last_gemm_tma = tma ? 1 : 0;
-  if (tma) {
-    static bool attr_tma = false;
-    if (!attr_tma) {
-      KPM_CUDA_TRY(cudaFuncSetAttribute(mu_gemm_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem));
-      attr_tma = true;
-    }
-    mu_gemm_tma_kernel<<<dim3(tiles, KS), kGemmThreads, kTmaSmem, s>>>(g, ma, mb);
-  } else {
-    mu_gemm_kernel<<<dim3(tiles, KS), kGemmThreads, kGemmSmem, s>>>(g);
+  bool tma = false;
+  if (want_tma)
+    tma = sw ? (operand_map_sw(&ma, A, lda, mt * kTile) && operand_map_sw(&mb, B, lda, mt * kTile))
+             : (operand_map(&ma, A, lda, mt * kTile) && operand_map(&mb, B, lda, mt * kTile));
+  g_last_gemm_tma = (tma ? 1 : 0) + (sw ? 2 : 0);
+  static bool attr[4] = {false, false, false, false};
+  const int which = (tma ? 1 : 0) + (sw ? 2 : 0);
+  if (!attr[which]) {
+    const void* fn = tma ? (sw ? (const void*)mu_gemm_tma_kernel<true> : (const void*)mu_gemm_tma_kernel<false>)
+                         : (sw ? (const void*)mu_gemm_kernel<true> : (const void*)mu_gemm_kernel<false>);
+    KPM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(tma ? kTmaSmem : kGemmSmem)));
+    attr[which] = true;
   }
+  if (tma && sw)
+    mu_gemm_tma_kernel<true><<<dim3(tiles, KS), kGemmThreads, kTmaSmem, s>>>(g, ma, mb);
+  else if (tma)
+    mu_gemm_tma_kernel<false><<<dim3(tiles, KS), kGemmThreads, kTmaSmem, s>>>(g, ma, mb);
+  else if (sw)
+    mu_gemm_kernel<true><<<dim3(tiles, KS), kGemmThreads, kGemmSmem, s>>>(g);
+  else
+    mu_gemm_kernel<false><<<dim3(tiles, KS), kGemmThreads, kGemmSmem, s>>>(g);
   KPM_CUDA_TRY(cudaGetLastError());
   mu_reduce_kernel<<<(Nm * Nm + 255) / 256, 256, 0, s>>>(g.part_hi, g.part_lo, KS, tiles, mt, Nm, scale, accumulate,
                                                          mu);

@@ -59,10 +59,8 @@ __host__ __device__ constexpr int ws_stages() {
   return (sizeof(T) == 8 && REAL && TPR == 1 && U == 1 && K == kWsFF) ? 3 : kWsStages;
 }
 
-// MINB > 0 asks for MINB resident CTAs per SM (a register bound the compiler meets with some
-// spilling); the autotuner times that form beside the default one (launch_ws_dense).
-template <typename T, bool REAL, int TPR, int VPT, int U, int K, int MINB = 0>
-__global__ void __launch_bounds__(kWsThreads, (MINB > 0 ? MINB : (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : 1)))
+template <typename T, bool REAL, int TPR, int VPT, int U, int K>
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : 1))
     cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;
@@ -343,11 +341,11 @@ __global__ void __launch_bounds__(kWsThreads, (MINB > 0 ? MINB : (U == 1 ? ((siz
   }
 }
 
-template <typename T, bool REAL, int TPR, int VPT, int U, int K, int MINB = 0>
+template <typename T, bool REAL, int TPR, int VPT, int U, int K>
 bool ws_smem_attr(size_t smem) {
   static size_t configured = 0;
   if (smem <= configured) return true;
-  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K, MINB>,
+  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -392,32 +390,15 @@ int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
   return KPM_OK;
 }
 
-// The one-set FP64 step with float-float moment products (K = kWsFF, real values, one row
-// per thread) compiled for four resident CTAs per SM instead of three: more warps to hide
-// the gathers, at the price of a few spilled registers.
-template <bool REAL, int TPR>
-int launch_ws_dense(const StepParams& p, int grid, cudaStream_t s) {
-  constexpr int kDense = 4;
-  const size_t smem = ws_stages<double, REAL, TPR, 1, kWsFF>() * staged_stage_bytes<double, REAL, TPR, 1, 1>(p.L, 2);
-  if (!ws_smem_attr<double, REAL, TPR, 1, 1, kWsFF, kDense>(smem)) return KPM_ERR_UNSUPPORTED;
-  cheb_next_ws_kernel<double, REAL, TPR, 1, 1, kWsFF, kDense><<<grid, kWsThreads, smem, s>>>(p);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    set_last_cuda_error(e);
-    return KPM_ERR_CUDA;
-  }
-  return KPM_OK;
-}
-
 // CTAs of one SM for epilogue variant K
-template <typename T, bool REAL, int TPR, int VPT, int U, int K, int MINB = 0>
+template <typename T, bool REAL, int TPR, int VPT, int U, int K>
 int ws_ctas_per_sm_k(int L, int nvec) {
   const size_t smem = ws_stages<T, REAL, TPR, U, K>() * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
   if (smem > 200 * 1024) return 0;
-  if (!ws_smem_attr<T, REAL, TPR, VPT, U, K, MINB>(smem)) return 0;
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U, K>(smem)) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K, MINB>,
-                                                    kWsThreads, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K>, kWsThreads,
+                                                    smem) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;
   }

@@ -157,22 +157,27 @@ def test_fused_velocity_step_matches_separate_products(cuda_lib, monkeypatch, R)
     assert np.max(np.abs(mu.cpu().numpy() - separate)) <= 1e-5 * np.max(np.abs(separate))
 
 
+VARIANTS = {"legacy": 2, "tma": 3, "legacy_plain": 0, "tma_plain": 1}  # kpm_mu_gemm_path: TMA bit, swizzle bit
+
+
 @pytest.mark.parametrize("nvec,Nm", [(8, 256), (4096, 64), (70000, 200), (300000, 256)])
-def test_tma_contraction_equals_thread_loaded_kernel(cuda_lib, monkeypatch, nvec, Nm):
-    """The contraction whose operand tiles come in through the TMA engine (mu_gemm_tma_kernel)
-    runs by default, and its moment matrix equals, bit for bit, that of the kernel whose
-    threads load the operands (KPM_MU_GEMM=legacy): the same MMAs in the same order."""
+def test_contraction_variants_agree_bit_for_bit(cuda_lib, monkeypatch, nvec, Nm):
+    """The four forms of the contraction kernel -- operand tiles loaded by the threads or by the
+    TMA engine, in the 64-byte-swizzled or the no-swizzle layout -- run the same MMAs on the
+    same values in the same order, so their moment matrices agree bit for bit; the default is
+    the threads' loads into the swizzled layout.  Each matches an FP64 product at 2e-5."""
     rng = np.random.default_rng(nvec + Nm)
     L = rng.normal(size=(256, 2 * nvec)).astype(np.float32)
     Rm = rng.normal(size=(256, 2 * nvec)).astype(np.float32)
-    mu_tma = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
-    assert cuda_lib.kpm_mu_gemm_path() == 1
-    monkeypatch.setenv("KPM_MU_GEMM", "legacy")
-    mu_old = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
-    assert cuda_lib.kpm_mu_gemm_path() == 0
+    mu_default = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
+    assert cuda_lib.kpm_mu_gemm_path() == VARIANTS["legacy"]
+    for name, path in VARIANTS.items():
+        monkeypatch.setenv("KPM_MU_GEMM", name)
+        mu = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
+        assert cuda_lib.kpm_mu_gemm_path() == path, name
+        assert np.array_equal(mu, mu_default), name
     monkeypatch.delenv("KPM_MU_GEMM")
-    assert np.array_equal(mu_tma, mu_old)
     Lc = L[:Nm, 0::2].astype(np.float64) + 1j * L[:Nm, 1::2]
     Rc = Rm[:Nm, 0::2].astype(np.float64) + 1j * Rm[:Nm, 1::2]
     ref = np.conj(Lc) @ Rc.T
-    assert np.max(np.abs(mu_tma - ref)) / np.max(np.abs(ref)) < 2e-5
+    assert np.max(np.abs(mu_default - ref)) / np.max(np.abs(ref)) < 2e-5

@@ -222,17 +222,14 @@ def test_long_recursion_crosses_moment_chunks(cuda_lib):
 
 
 @pytest.mark.parametrize("doubled", [False, True])
-@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2", "ws1", "ws2", "ws1dense"])
+@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2", "ws1", "ws2"])
 @pytest.mark.parametrize("dtype,R", [("c128", 8), ("c128", 1), ("c128", 4), ("c64", 2), ("c64", 8), ("c64", 1)])
 def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R, doubled):
     """Each recursion-step kernel the autotuner can pick, forced, against the oracle
     (complex128 at 1e-10; complex64 at its own precision), for the direct recursion
-    and for doubled moments (which the staged kernels do not serve).  ws1dense is the
-    float-float-products FP64 step at four CTAs per SM (one moment set, complex128)."""
+    and for doubled moments (which the staged kernels do not serve)."""
     if doubled and kernel.startswith("staged"):
         pytest.skip("doubled moments run on the grid-stride and producer-warp kernels")
-    if kernel == "ws1dense" and (doubled or dtype != "c128"):
-        pytest.skip("the four-CTA form serves the complex128 one-set step")
     from minijclsquant_gb300 import _capi, device, lattice
     from minijclsquant_gb300.modifiers import modifier_bounds
     from minijclsquant_gb300.observables import random_vector_generator
@@ -249,7 +246,7 @@ def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R, doub
     code = _capi.KPM_C128 if dtype == "c128" else _capi.KPM_C64
     assert cuda_lib.kpm_ell_step_config(op.handle, code, R, ctypes.byref(kind), ctypes.byref(U), None, None) == 0
     assert (kind.value, U.value) == {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2), "ws1": (2, 1),
-                                     "ws2": (2, 2), "ws1dense": (3, 1)}[kernel]
+                                     "ws2": (2, 2)}[kernel]
     assert cuda_lib.kpm_ell_check(op.handle, None) == 0
     for r in range(R):
         ref = oracle.rec_A_tab(150, Hk.data, Hk.indices, Hk.len_row, vs[r])

@@ -688,6 +688,7 @@ def run_batched(a, hbm_peak, steps, warmup):
                                                            W_range=(0.0, 2.0), seed=42)
     B = batched.BatchedELL(datas, idxs, L)
     setup_s = time.perf_counter() - t0
+    cpu_sample = [(datas[k], idxs[k]) for k in range(min(8, len(datas)))]
     del datas, idxs
     R, M = a.batch_R, a.batch_M
     v = torch.from_numpy(batched.ensemble_vectors(B.rows, R)).cuda()
@@ -734,8 +735,30 @@ def run_batched(a, hbm_peak, steps, warmup):
     exec_steps = executed_steps(M, doubled) + 1
     exec_rate = float(B.n_total) * R * exec_steps / (ms64 * 1e-3)
     ach = bytes_per_site_step * exec_rate / 1e9
+    cpu = None
+    if not a.no_cpu:
+        # the reference's way through an ensemble: one rec_A_tab per instance and vector
+        # (jclsquant/recurrence_functions.py:9-40 over its own aAxby / vdot), on the first
+        # instances of the ensemble at reduced M, per site-step
+        threads = os.cpu_count() or 1
+        Mc, site_steps_c, t_c, kind_c = 64, 0.0, 0.0, "port"
+        vcpu = batched.ensemble_vectors(np.array([d.size // L for d, _ in cpu_sample]), R)
+        off = 0
+        for d, ix in cpu_sample:
+            nk = d.size // L
+            prob_k = {"n": nk, "L": L, "data_kpm": np.ascontiguousarray(d), "indices": np.ascontiguousarray(ix)}
+            for r in range(R):
+                dt_k, kind_c = cpu_rec_A_tab(Mc, prob_k, np.ascontiguousarray(vcpu[r, off:off + nk]), threads)
+                t_c += dt_k
+                site_steps_c += nk * (Mc - 1)
+            off += nk
+        cpu = {"value": site_steps_c / t_c, "unit": UNIT, "cores": threads, "kind": kind_c,
+               "sample": "rec_A_tab loop per instance and vector, the first %d instances (%d sites), R=%d, M=%d "
+                         "(%.2f s)" % (len(cpu_sample), int(sum(d.size // L for d, _ in cpu_sample)), R, Mc, t_c),
+               "gpu_c64_over_cpu": val64 / (site_steps_c / t_c)}
     return {"workload": "%d honeycomb instances, sides U{32..%d} cells (%d sites total), W~U[0,2] eV, R=%d, M=%d"
                         % (B.n_inst, a.batch_side_max, B.n_total, R, M),
+            "cpu_baseline": cpu,
             "value": val64, "unit": UNIT, "ms_per_step": ms64, "dtype": "c64 recursion, f64 moment accumulation",
             "hbm_gbs": ach, "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s",
                                          "frac": ach / hbm_peak, "bytes_per_site_step": bytes_per_site_step},

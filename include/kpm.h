@@ -248,9 +248,11 @@ int kpm_adjoint_backward_ex(kpm_ell* h, const double* c, double* grad, int dtype
  * kpm_cheb_table: tab[m] = T_m(H) v, m < M (the recursion of rec_A_tab,
  *   jclsquant/recurrence_functions.py:9-40, with every vector kept); with s_op also
  *   stab[m] = S T_m(H) v from the same gathers (stab must then be given, else NULL).
+ *   v may be row 0 of tab; tab and stab may not overlap (KPM_ERR_INVALID_ARG).
  * kpm_cheb_clenshaw_table: the reverse recursion lam_k = S z_k + 2 H lam_{k+1} - lam_{k+2}
  *   (k = M-1 .. 1), lam_0 = S z_0 + H lam_1 - lam_2, lam_M = lam_{M+1} = 0, all rows kept
- *   (S = identity when s_op is NULL).  lam_0 = sum_k T_k(H) S z_k (Clenshaw), and for a
+ *   (S = identity when s_op is NULL; z and lam may not overlap).  lam_0 = sum_k T_k(H) S z_k
+ *   (Clenshaw), and for a
  *   functional Re sum_k (S z_k)^H T_k(H) w the rows are its adjoint vectors: the derivative
  *   by the entry (i, j) of H is sum_{k <= M-2} c_k conj(lam_{k+1}[i]) (T_k(H) w)[j], c_0 = 1,
  *   c_k = 2 (kpm_ell_slot_sum).

@@ -105,6 +105,12 @@ __global__ void __launch_bounds__(256) table_step_kernel(const TableStep p) {
   }
 }
 
+// Whether two device ranges of `bytes` bytes each share memory.
+bool overlap(const void* a, const void* b, size_t bytes) {
+  const uintptr_t x = reinterpret_cast<uintptr_t>(a), y = reinterpret_cast<uintptr_t>(b);
+  return x < y + bytes && y < x + bytes;
+}
+
 int grid_rows(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>((n + 255) / 256, 8192)); }
 
 int launch_table_step(bool rh, bool rs, const TableStep& p, cudaStream_t s) {
@@ -167,7 +173,11 @@ int kpm_cheb_table(kpm_ell* h, kpm_ell* s_op, int M, const double* v, double* ta
   const int64_t n = h->n;
   double2* T = reinterpret_cast<double2*>(tab);
   double2* ST = reinterpret_cast<double2*>(stab);
-  KPM_CUDA_TRY(cudaMemcpyAsync(T, v, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  if (s_op && overlap(tab, stab, (size_t)M * n * sizeof(double2))) return KPM_ERR_INVALID_ARG;
+  if (v != tab) {  // v may be row 0 of the table itself
+    if (overlap(v, tab, (size_t)n * sizeof(double2))) return KPM_ERR_INVALID_ARG;
+    KPM_CUDA_TRY(cudaMemcpyAsync(T, v, (size_t)n * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+  }
   TableStep p{};
   p.vh = h->val64;
   p.ch = h->col;
@@ -204,6 +214,8 @@ int kpm_cheb_table(kpm_ell* h, kpm_ell* s_op, int M, const double* v, double* ta
 int kpm_cheb_clenshaw_table(kpm_ell* h, kpm_ell* s_op, int M, const double* z, double* lam, void* stream) {
   if (!h || !z || !lam || M < 1) return KPM_ERR_INVALID_ARG;
   if (s_op && (s_op->n != h->n || s_op->n_pad != h->n_pad)) return KPM_ERR_SHAPE;
+  // every row of z is gathered while rows of lam are written: the two may not share memory
+  if (overlap(z, lam, (size_t)M * h->n * sizeof(double2))) return KPM_ERR_INVALID_ARG;
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   const int64_t n = h->n;
   const double2* Z = reinterpret_cast<const double2*>(z);

@@ -688,7 +688,7 @@ def run_batched(a, hbm_peak, steps, warmup):
                                                            W_range=(0.0, 2.0), seed=42)
     B = batched.BatchedELL(datas, idxs, L)
     setup_s = time.perf_counter() - t0
-    cpu_sample = [(datas[k], idxs[k]) for k in range(min(8, len(datas)))]
+    cpu_sample = [(datas[k], idxs[k]) for k in range(min(16, len(datas)))]
     del datas, idxs
     R, M = a.batch_R, a.batch_M
     v = torch.from_numpy(batched.ensemble_vectors(B.rows, R)).cuda()
@@ -741,7 +741,7 @@ def run_batched(a, hbm_peak, steps, warmup):
         # (jclsquant/recurrence_functions.py:9-40 over its own aAxby / vdot), on the first
         # instances of the ensemble at reduced M, per site-step
         threads = os.cpu_count() or 1
-        Mc, site_steps_c, t_c, kind_c = 64, 0.0, 0.0, "port"
+        Mc, site_steps_c, t_c, kind_c = 512, 0.0, 0.0, "port"
         vcpu = batched.ensemble_vectors(np.array([d.size // L for d, _ in cpu_sample]), R)
         off = 0
         for d, ix in cpu_sample:

@@ -460,8 +460,9 @@ int kpm_measure_fp64_fma_rate(double* fma_per_second, void* stream);
  * kpm_mu_contract) ran: bit 0 = operand tiles brought in by the TMA engine
  * (mu_gemm_tma_kernel) rather than loaded by the threads (mu_gemm_kernel); bit 1 = the
  * 64-byte-swizzled shared-memory operand layout rather than the no-swizzle one; -1 =
- * none yet.  KPM_MU_GEMM=legacy|tma|legacy_plain|tma_plain picks one (default: legacy,
- * swizzled). */
+ * none yet.  KPM_MU_GEMM=legacy|tma|legacy_plain|tma_plain picks one (default: tma_plain,
+ * the TMA engine into the no-swizzle layout; the threads' loads when the driver offers no
+ * tensor-map encoder).  All four give bit-identical results. */
 int kpm_mu_gemm_path(void);
 
 #ifdef __cplusplus

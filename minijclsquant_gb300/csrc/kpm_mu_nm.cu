@@ -101,6 +101,44 @@ __device__ __forceinline__ float4 tf32x4(float4 x) {
   return make_float4(to_tf32(x.x), to_tf32(x.y), to_tf32(x.z), to_tf32(x.w));
 }
 
+// Adds a thread's level-1 sums run[] (one TMEM lane, kColsPerThread columns; column c at
+// ohi[c * kTile]) into its float-float partial (TwoSum into hi, the rounding error into lo)
+// and restarts them.  The columns go in batches of kFlushBatch whose loads are all issued
+// before any of the batch's stores: one store may alias a later column's load as far as the
+// compiler knows, so column-by-column code waits a full global round trip per column
+// (64 per flush, about a quarter of the contraction time at the Kubo size).
+constexpr int kFlushBatch = 8;
+__device__ __forceinline__ void flush_partials(float (&run)[kColsPerThread], float* ohi, float* olo, bool first) {
+#pragma unroll
+  for (int c0 = 0; c0 < kColsPerThread; c0 += kFlushBatch) {
+    if (first) {
+#pragma unroll
+      for (int i = 0; i < kFlushBatch; ++i) {
+        ohi[(c0 + i) * kTile] = run[c0 + i];
+        olo[(c0 + i) * kTile] = 0.f;
+      }
+    } else {
+      float a[kFlushBatch], l[kFlushBatch];
+#pragma unroll
+      for (int i = 0; i < kFlushBatch; ++i) {
+        a[i] = ohi[(c0 + i) * kTile];
+        l[i] = olo[(c0 + i) * kTile];
+      }
+#pragma unroll
+      for (int i = 0; i < kFlushBatch; ++i) {
+        const float b = run[c0 + i];
+        const float s = __fadd_rn(a[i], b);
+        const float bp = __fsub_rn(s, a[i]);
+        const float e = __fadd_rn(__fsub_rn(a[i], __fsub_rn(s, bp)), __fsub_rn(b, bp));
+        ohi[(c0 + i) * kTile] = s;
+        olo[(c0 + i) * kTile] = __fadd_rn(l[i], e);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < kFlushBatch; ++i) run[c0 + i] = 0.f;
+  }
+}
+
 // One CTA: output tile (n0.., m0..) of 128 x 128, Re and Im side by side as one
 // M = 128, N = 256 MMA against BX = [B rows; B rows with (re, im) -> (im, -re)],
 // over its K range.  The MMA accumulator is restarted every kChainTiles K tiles,
@@ -182,21 +220,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmPara
   };
   // level-1 sums into the float-float partial (TwoSum), then restart them
   auto flush_l2 = [&]() {
-#pragma unroll
-    for (int c = 0; c < kColsPerThread; ++c) {
-      if (first_flush) {
-        ohi[c * kTile] = run[c];
-        olo[c * kTile] = 0.f;
-      } else {
-        const float a = ohi[c * kTile], b = run[c];
-        const float s = __fadd_rn(a, b);
-        const float bp = __fsub_rn(s, a);
-        const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
-        ohi[c * kTile] = s;
-        olo[c * kTile] = __fadd_rn(olo[c * kTile], e);
-      }
-      run[c] = 0.f;
-    }
+    flush_partials(run, ohi, olo, first_flush);
     first_flush = false;
   };
 
@@ -429,21 +453,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     return true;
   };
   auto flush_l2 = [&]() {
-#pragma unroll
-    for (int c = 0; c < kColsPerThread; ++c) {
-      if (first_flush) {
-        ohi[c * kTile] = run[c];
-        olo[c * kTile] = 0.f;
-      } else {
-        const float a = ohi[c * kTile], b = run[c];
-        const float s = __fadd_rn(a, b);
-        const float bp = __fsub_rn(s, a);
-        const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bp)), __fsub_rn(b, bp));
-        ohi[c * kTile] = s;
-        olo[c * kTile] = __fadd_rn(olo[c * kTile], e);
-      }
-      run[c] = 0.f;
-    }
+    flush_partials(run, ohi, olo, first_flush);
     first_flush = false;
   };
 
@@ -648,12 +658,13 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
   g.part_lo = part + (size_t)KS * tiles * 2 * kTileElems;
   g.err = err;
   // kernel: operand tiles loaded by the threads ("legacy") or by the TMA engine ("tma"), in the
-  // 64-byte-swizzled layout or the no-swizzle one ("_plain"); KPM_MU_GEMM picks one, the default
-  // is the threads' loads into the swizzled layout
+  // 64-byte-swizzled layout or the no-swizzle one ("_plain"); KPM_MU_GEMM picks one.  The
+  // default is the TMA engine into the no-swizzle layout (the fastest measured; the threads'
+  // loads take it when the tensor-map encoder is unavailable)
   const char* force = getenv("KPM_MU_GEMM");
   const std::string f = force ? force : "";
-  const bool want_tma = f == "tma" || f == "tma_plain";
-  const bool sw = !(f == "legacy_plain" || f == "tma_plain");
+  const bool want_tma = !(f == "legacy" || f == "legacy_plain");
+  const bool sw = f == "legacy" || f == "tma";
   CUtensorMap ma, mb;
   bool tma = false;
   if (want_tma)

@@ -165,12 +165,12 @@ def test_contraction_variants_agree_bit_for_bit(cuda_lib, monkeypatch, nvec, Nm)
     """The four forms of the contraction kernel -- operand tiles loaded by the threads or by the
     TMA engine, in the 64-byte-swizzled or the no-swizzle layout -- run the same MMAs on the
     same values in the same order, so their moment matrices agree bit for bit; the default is
-    the threads' loads into the swizzled layout.  Each matches an FP64 product at 2e-5."""
+    the TMA engine's loads into the no-swizzle layout.  Each matches an FP64 product at 2e-5."""
     rng = np.random.default_rng(nvec + Nm)
     L = rng.normal(size=(256, 2 * nvec)).astype(np.float32)
     Rm = rng.normal(size=(256, 2 * nvec)).astype(np.float32)
     mu_default = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()
-    assert cuda_lib.kpm_mu_gemm_path() == VARIANTS["legacy"]
+    assert cuda_lib.kpm_mu_gemm_path() == VARIANTS["tma_plain"]
     for name, path in VARIANTS.items():
         monkeypatch.setenv("KPM_MU_GEMM", name)
         mu = _contract(cuda_lib, L, Rm, Nm).cpu().numpy()

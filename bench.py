@@ -1087,6 +1087,8 @@ def run_kubo(a, peaks, steps, warmup):
     ref = _fp64_mu_block(Hk.data, Vk, Hk.indices, Hk.len_row, vs[0], sel)
     err = float(np.max(np.abs(got - ref)) / np.max(np.abs(ref)))
     rec_site_steps = float(n) * R * 3 * Nm  # L and R recursions plus the V products, per vector
+    path = lib.kpm_mu_gemm_path()  # bit 0: TMA-fed operand tiles, bit 1: 64-byte-swizzled layout
+    gemm = ("mu_gemm_tma_kernel" if path & 1 else "mu_gemm_kernel") + (" (swizzled" if path & 2 else " (no-swizzle")
     return {"workload": "Kubo-Greenwood mu_nm: honeycomb %dx%d cells (%d sites), W=1 eV, V_x, Nm=%d, R=%d"
                         % (cells, cells, n, Nm, R),
             "ms_per_mu_nm": ms, "site_steps_per_s": rec_site_steps / (ms * 1e-3), "setup_s": setup_s,
@@ -1094,7 +1096,7 @@ def run_kubo(a, peaks, steps, warmup):
                             "roofline": {"bound": "tensor", "achieved": ach, "peak": tf32_peak, "unit": "TFLOP/s",
                                          "frac": ach / tf32_peak,
                                          "peak_source": "TF32 dense = half of MEASURED_PEAKS.json bf16_tflops"},
-                            "kernel": "mu_gemm_kernel (tcgen05.mma kind::tf32, 3xTF32, TMEM accumulators)"},
+                            "kernel": gemm + " layout; tcgen05.mma kind::tf32, 3xTF32, TMEM accumulators)"},
             "fp64_check": {"block": "n, m in %s, vector 0" % sel, "max_abs_err_over_max": err}}
 
 

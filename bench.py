@@ -325,7 +325,8 @@ def run_time_evolution(a, op, n, L, prob, hbm_peak, world):
     kind, rpt, grid, us = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
     _capi.check(lib.kpm_ell_series_config(op.handle, _capi.KPM_C128, R2, ctypes.byref(kind), ctypes.byref(rpt),
                                           ctypes.byref(grid), ctypes.byref(us)))
-    kname = ("cheb_next_ws_kernel<SER> (producer warp, %d row(s)/thread)" % rpt.value if kind.value == 2
+    kname = ("cheb_next_ws_kernel<SER> (producer warp, %d row(s)/thread%s)"
+             % (rpt.value, ", two sub-tiles per stage" if kind.value == 3 else "") if kind.value in (2, 3)
              else "cheb_step_kernel (grid-stride, MODE_NEXT STORE|SERIES)")
     blk = {"value": float(n) * R2 * (M2 - 1) * len_t * world / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
            "config": {"vectors": "U, U_c", "M2": M2, "len_t": len_t, "dt": a.time_dt, "sites": n},
@@ -1144,7 +1145,8 @@ def run_fp64_products(a, op, v, M, R, n, bytes_per_launch, hbm_peak, fma_peak, r
            "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm_peak, "unit": "GB/s", "frac": gbs / hbm_peak,
                         "kernel": "%s (FP64 moment products, %d row(s)/thread)"
                                   % ({0: "cheb_step_kernel", 1: "cheb_next_staged_kernel",
-                                      2: "cheb_next_ws_kernel"}.get(kind.value, "?"), rpt.value),
+                                      2: "cheb_next_ws_kernel", 3: "cheb_next_ws_kernel (two sub-tiles per stage)"}
+                                     .get(kind.value, "?"), rpt.value),
                         "grid": grid.value, "avg_launch_ms": launch_s * 1e3},
            "fp64": {"achieved_fma_per_s": fma, "peak_fma_per_s": fma_peak, "frac": fma / fma_peak,
                     "fma_per_site_step": rec_fma + 4},
@@ -1315,7 +1317,9 @@ def run_ours(a):
     _capi.check(lib.kpm_ell_step_config(op.handle, _capi.dtype_code(a.dtype), R, ctypes.byref(kind), ctypes.byref(rpt),
                                         ctypes.byref(grid), ctypes.byref(us)))
     kname = {1: "cheb_next_staged_kernel (bulk-copy staged, %d row(s)/thread)" % rpt.value,
-             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value}.get(
+             2: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread)" % rpt.value,
+             3: "cheb_next_ws_kernel (bulk-copy staged, producer warp, %d row(s)/thread, two sub-tiles per stage)"
+                % rpt.value}.get(
         kind.value, "cheb_step_kernel (grid-stride, MODE_NEXT STORE|MOM1)")
     roofline = {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved_gbs / hbm_peak, "traffic": traffic, "peak_source": peak_src,
@@ -1326,7 +1330,7 @@ def run_ours(a):
     # FP64 FMAs per site-step: the recursion's 2L (real values) or 4L, plus the moment's 4 unless
     # the producer-warp kernel forms the moment products in float-float arithmetic (the default
     # for one moment set; KPM_MOMENTS_FP64=1 turns it off)
-    ff_products = (a.dtype == "c128" and not doubled and kind.value == 2
+    ff_products = (a.dtype == "c128" and not doubled and kind.value in (2, 3)
                    and os.environ.get("KPM_MOMENTS_FP64", "") in ("", "0"))
     rec_fma = 2 * L if op.is_real else 4 * L
     fma_per_site_step = rec_fma + (6 if doubled else (0 if ff_products else 4))

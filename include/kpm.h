@@ -96,17 +96,19 @@ int kpm_ell_reserve(kpm_ell* h, int dtype, int R, int M);
  * device (KPM_ERR_TIMEOUT if a bounded wait ran out), then clear it. */
 int kpm_ell_check(kpm_ell* h, void* stream);
 /* The recursion-step kernel chosen for (dtype, R): kind 0 = grid-stride,
- * 1 = bulk-copy staged, 2 = bulk-copy staged with a producer warp; rows per
- * thread per tile; CTAs; measured us per step.  A choice is timed once per
+ * 1 = bulk-copy staged, 2 = bulk-copy staged with a producer warp, 3 = the
+ * producer-warp kernel with two sub-tiles per shared-memory stage (complex128);
+ * rows per thread per tile; CTAs; measured us per step.  A choice is timed once per
  * operator shape and column structure in a process and shared by later handles
- * (KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2 forces one and bypasses that).
+ * (KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2|ws1s2 forces one and bypasses that).
  * Operators of at most 2^20 / R padded rows (L2-resident recursions, where launch
  * latency sets the pace) replay each recursion of kpm_cheb_moments as one CUDA graph
  * launch, recorded on first use per shape (KPM_NO_GRAPH=1 launches step by step). */
 int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                         float* step_us);
 /* The same for the series step (kpm_cheb_series, kpm_time_evolve, kpm_time_sigma):
- * kind 0 = grid-stride or 2 = producer warp, timed on the operator at first use. */
+ * kind 0 = grid-stride, 2 = producer warp or 3 = producer warp with two sub-tiles per
+ * stage (complex128), timed on the operator at first use. */
 int kpm_ell_series_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_thread, int* grid,
                           float* step_us);
 /* Doubling (opt-in: KPM_FLAG_DOUBLING at creation or kpm_ell_set_doubling).

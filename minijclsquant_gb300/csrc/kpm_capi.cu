@@ -110,7 +110,7 @@ int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepPar
   if (cfg.kind == 1)
     return f32 ? launch_staged_f32(real, R, cfg.U, p, cfg.grid, s) : launch_staged_f64(real, R, cfg.U, p, cfg.grid, s);
   if (cfg.kind == 2)
-    return f32 ? launch_ws_f32(real, R, cfg.U, p, cfg.grid, s) : launch_ws_f64(real, R, cfg.U, p, cfg.grid, s);
+    return f32 ? launch_ws_f32(real, R, cfg.U, p, cfg.grid, s) : launch_ws_f64(real, R, cfg.U, p, cfg.grid, s, cfg.sb);
   return launch_step(f32, real, R, MODE_NEXT, EPI_STORE | (series ? EPI_SERIES : EPI_MOM1), p, cfg.grid, s);
 }
 
@@ -119,7 +119,9 @@ int launch_next(bool f32, bool real, int R, const StepConfig& cfg, const StepPar
 // producer-warp form, each with 1 or 2 rows per thread and a full wave of
 // resident CTAs.  When several fit, each is timed on the operator itself (a few
 // launches on zeroed workspace vectors) and the fastest is kept for the
-// handle's lifetime.  KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2 forces one.
+// handle's lifetime.  Complex128 adds the producer-warp form with two sub-tiles per stage
+// (ws1s2: twice the rows per bulk copy, the same registers as ws1).
+// KPM_STEP_KERNEL=simple|staged1|staged2|ws1|ws2|ws1s2 forces one.
 // sets: 1 one moment set, 2 two sets, 3 doubled moments, 4 a series step (no
 // moments; series += c_m T_{m+1}).  Timing clears ws.ta, ws.tb and ws.vl (and ws.vr
 // for sets 2 and 3): callers tune before they fill those.
@@ -177,18 +179,24 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
   // doubled moments (sets == 3) and series steps (sets == 4) the grid-stride and the
   // producer-warp kernels
   for (int kind = 1; kind <= 2 && sets != 2; ++kind)
-    for (int U = 1; U <= 2; ++U) {
+    for (int U = 1; U <= 3; ++U) {
+      // U = 3 stands for one row per thread with two sub-tiles per stage (producer-warp, complex128)
+      const int sb = U == 3 ? 2 : 1;
+      const int u = U == 3 ? 1 : U;
+      if (U == 3 && (kind == 1 || f32)) continue;
       if ((sets == 3 || sets == 4) && kind == 1) continue;
-      if (!f.empty() && f != std::string(kind == 1 ? "staged" : "ws") + (U == 1 ? "1" : "2")) continue;
-      const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, U, h->L, 2)
-                                       : staged_ctas_f64(h->is_real, Rg, U, h->L, 2))
-                                : (f32 ? ws_ctas_f32(h->is_real, Rg, U, h->L, 2)
-                                       : ws_ctas_f64(h->is_real, Rg, U, h->L, 2, ffm));
+      const std::string name = std::string(kind == 1 ? "staged" : "ws") + (U == 2 ? "2" : "1") + (sb == 2 ? "s2" : "");
+      if (!f.empty() && f != name) continue;
+      const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, u, h->L, 2)
+                                       : staged_ctas_f64(h->is_real, Rg, u, h->L, 2))
+                                : (f32 ? ws_ctas_f32(h->is_real, Rg, u, h->L, 2)
+                                       : ws_ctas_f64(h->is_real, Rg, u, h->L, 2, ffm, sb));
       if (occ <= 0) continue;
-      const int64_t ntiles = h->n_pad / staged_tile_rows(f32, Rg, U);
+      const int64_t ntiles = h->n_pad / (staged_tile_rows(f32, Rg, u) * sb);
       StepConfig c;
       c.kind = kind;
-      c.U = U;
+      c.U = u;
+      c.sb = sb;
       c.grid = (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)occ * h->sm_count));
       cands.push_back(c);
     }
@@ -1265,7 +1273,7 @@ int kpm_ell_step_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per_t
   if (dtype == KPM_C64) KPM_TRY(ensure_f32_values(h, nullptr));
   StepConfig cfg;
   KPM_TRY(step_config(h, dtype == KPM_C64, Rg, use_doubling(h, 4) ? 3 : 1, nullptr, &cfg));
-  if (kind) *kind = cfg.kind;
+  if (kind) *kind = (cfg.kind == 2 && cfg.sb == 2) ? 3 : cfg.kind;
   if (rows_per_thread) *rows_per_thread = cfg.U;
   if (grid) *grid = cfg.grid;
   if (step_us) *step_us = cfg.us;
@@ -1278,7 +1286,7 @@ int kpm_ell_series_config(kpm_ell* h, int dtype, int R, int* kind, int* rows_per
   if (dtype == KPM_C64) KPM_TRY(ensure_f32_values(h, nullptr));
   StepConfig cfg;
   KPM_TRY(step_config(h, dtype == KPM_C64, pow2_group(R), 4, nullptr, &cfg));
-  if (kind) *kind = cfg.kind;
+  if (kind) *kind = (cfg.kind == 2 && cfg.sb == 2) ? 3 : cfg.kind;
   if (rows_per_thread) *rows_per_thread = cfg.U;
   if (grid) *grid = cfg.grid;
   if (step_us) *step_us = cfg.us;

@@ -31,12 +31,13 @@ int staged_ctas_f64(bool real, int R, int U, int L, int nvec) {
   return Staged<double>::ctas_per_sm(real, R, U, L, nvec);
 }
 
-int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
-  return Ws<double>::launch(real, R, U, p, grid, s);
+int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s, int sb) {
+  return Ws<double>::launch(real, R, U, p, grid, s, sb);
 }
 
-int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff) {
-  return Ws<double>::ctas_per_sm(real, R, U, L, nvec, ff);
+int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff, int sb) {
+  (void)nvec;
+  return Ws<double>::ctas_per_sm(real, R, U, L, ff, sb);
 }
 
 

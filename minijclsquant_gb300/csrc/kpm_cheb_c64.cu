@@ -38,7 +38,8 @@ int launch_ws_f32(bool real, int R, int U, const StepParams& p, int grid, cudaSt
 }
 
 int ws_ctas_f32(bool real, int R, int U, int L, int nvec) {
-  return Ws<float>::ctas_per_sm(real, R, U, L, nvec);
+  (void)nvec;
+  return Ws<float>::ctas_per_sm(real, R, U, L);
 }
 
 }  // namespace kpm

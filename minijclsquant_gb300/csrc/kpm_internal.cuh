@@ -91,6 +91,7 @@ struct MomentGraph {
 struct StepConfig {
   int kind = 0;  // 0: grid-stride kernel, 1: bulk-copy staged kernel, 2: staged with a producer warp
   int U = 1;     // rows per thread per tile (staged)
+  int sb = 1;    // sub-tiles of TILE rows per shared-memory stage (producer-warp kernel, complex128)
   int grid = 0;  // CTAs
   float us = 0;  // measured time of one step launch when tuned
 };
@@ -190,10 +191,10 @@ int launch_staged_f32(bool real, int R, int U, const StepParams& p, int grid, cu
 int staged_ctas_f64(bool real, int R, int U, int L, int nvec);
 int staged_ctas_f32(bool real, int R, int U, int L, int nvec);
 // The same step with a producer warp and full/empty stage barriers (kpm_ws.cuh).
-int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
+int launch_ws_f64(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s, int sb = 1);
 int launch_ws_f32(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s);
 // ff: CTAs of the float-float-products variant (one moment set, FP64 recursion)
-int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff = false);
+int ws_ctas_f64(bool real, int R, int U, int L, int nvec, bool ff = false, int sb = 1);
 int ws_ctas_f32(bool real, int R, int U, int L, int nvec);
 // Driver helpers (kpm_capi.cu).
 int pow2_group(int remaining);

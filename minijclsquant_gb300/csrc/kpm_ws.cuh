@@ -54,23 +54,24 @@ constexpr int kWsDbl = 3;     // doubled moments (two sets per step)
 
 // Shared-memory stages of one instantiation: three for the one-vector float-float step of a
 // real operator (three of its 20 KB stages per CTA let three CTAs share an SM), four otherwise.
-template <typename T, bool REAL, int TPR, int U, int K>
+template <typename T, bool REAL, int TPR, int U, int K, int SB = 1>
 __host__ __device__ constexpr int ws_stages() {
-  return (sizeof(T) == 8 && REAL && TPR == 1 && U == 1 && K == kWsFF) ? 3 : kWsStages;
+  return ((sizeof(T) == 8 && REAL && TPR == 1 && U == 1 && K == kWsFF) || SB > 1) ? 3 : kWsStages;
 }
 
-template <typename T, bool REAL, int TPR, int VPT, int U, int K>
-__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : 1))
+template <typename T, bool REAL, int TPR, int VPT, int U, int K, int SB = 1>
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : ((sizeof(T) == 8 && REAL && TPR >= 2) ? 2 : 1)))
     cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;
   constexpr int R = TPR * VPT;
   constexpr int RPB = kBlock / TPR;
   constexpr int TILE = RPB * U;
+  constexpr int STILE = TILE * SB;  // rows of one stage: SB sub-tiles of TILE rows
   constexpr bool F32 = std::is_same<T, float>::value;
   constexpr bool SER = K == kWsSeries;
   constexpr bool DBL = K == kWsDbl;
-  constexpr int NST = ws_stages<T, REAL, TPR, U, K>();
+  constexpr int NST = ws_stages<T, REAL, TPR, U, K, SB>();
   constexpr int kFlush = 8;
   constexpr int kWarps = kBlock / 32;
 
@@ -80,12 +81,12 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   __shared__ double2 red[kWarps * R];
 
   const int L = p.L;
-  const uint32_t col_b = (uint32_t)align16((size_t)L * TILE * 4);
-  const uint32_t val_b = (uint32_t)align16((size_t)L * TILE * sizeof(MV));
-  const uint32_t vec_b = (uint32_t)(TILE * TPR * sizeof(Raw));
+  const uint32_t col_b = (uint32_t)align16((size_t)L * STILE * 4);
+  const uint32_t val_b = (uint32_t)align16((size_t)L * STILE * sizeof(MV));
+  const uint32_t vec_b = (uint32_t)(STILE * TPR * sizeof(Raw));
   const uint32_t stage_b = col_b + val_b + 2 * vec_b;
 
-  const int ntiles = (int)(p.n_pad / TILE);
+  const int ntiles = (int)(p.n_pad / STILE);
   const int seg_tb = (int)(((int64_t)blockIdx.x * ntiles) / gridDim.x);
   const int seg_te = (int)(((int64_t)(blockIdx.x + 1) * ntiles) / gridDim.x);
   // kernel-parameter fields read in the tile loop are copied to registers first (a
@@ -120,14 +121,14 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       tc.vl2 = nullptr;
       tc.ld = p.ld;
       tc.L = L;
-      tc.col_slab = TILE * 4;
-      tc.val_slab = (uint32_t)(TILE * sizeof(MV));
+      tc.col_slab = STILE * 4;
+      tc.val_slab = (uint32_t)(STILE * sizeof(MV));
       tc.vec_slab = vec_b;
-      tc.vl_slab = DBL ? (uint32_t)(TILE * R * sizeof(T)) : vec_b;
+      tc.vl_slab = DBL ? (uint32_t)(STILE * R * sizeof(T)) : vec_b;
       if (DBL) tc.vl = static_cast<const unsigned char*>(p.hv);
       tc.col_b = col_b;
       tc.val_b = val_b;
-      tc.tx_bytes = (uint32_t)L * TILE * 4 + (uint32_t)L * TILE * (uint32_t)sizeof(MV) + vec_b + (tc.vl ? tc.vl_slab : 0);
+      tc.tx_bytes = (uint32_t)L * STILE * 4 + (uint32_t)L * STILE * (uint32_t)sizeof(MV) + vec_b + (tc.vl ? tc.vl_slab : 0);
       int issued = 0;
       for (int k = 0; k < my_count; ++k) {
         const int st = k % NST;
@@ -139,7 +140,7 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
         if (k == 0 && p.withhold_first)  // test hook: the stage is armed, its copies never issued
           mbar_arrive_expect_tx(&full[st], tc.tx_bytes);
         else
-          issue_tile(tc, smem + st * stage_b, &full[st], tile_of(k) * TILE, TPR * (int)sizeof(Raw), pol);
+          issue_tile(tc, smem + st * stage_b, &full[st], tile_of(k) * STILE, TPR * (int)sizeof(Raw), pol);
         issued = k + 1;
       }
       // copies of the last stages may still be landing: wait for them before leaving
@@ -198,13 +199,19 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
     for (int q = 0; q < VPT; ++q) mr[q] = mi[q] = mr2[q] = 0.0;
   };
 
-  for (int k = 0; k < my_count; ++k) {
+  // one iteration per sub-tile: stage k = it / SB, sub-tile sb = it % SB (the stage's wait
+  // comes with its first sub-tile, its release with its last)
+  for (int it = 0; it < my_count * SB; ++it) {
+    const int k = it / SB, sb = it % SB;
     const int st = k % NST;
-    bool ok = !dead && mbar_wait_bounded(&full[st], (uint32_t)((k / NST) & 1), p.wait_budget);
-    ok = __all_sync(0xffffffffu, ok);
-    if (!ok && !dead) {
-      if (lane == 0) atomicExch(p.err, KPM_ERR_TIMEOUT);
-      dead = true;
+    bool ok = !dead;
+    if (sb == 0) {
+      ok = ok && mbar_wait_bounded(&full[st], (uint32_t)((k / NST) & 1), p.wait_budget);
+      ok = __all_sync(0xffffffffu, ok);
+      if (!ok && !dead) {
+        if (lane == 0) atomicExch(p.err, KPM_ERR_TIMEOUT);
+        dead = true;
+      }
     }
     if (ok) {
       const unsigned char* base = smem + st * stage_b;
@@ -212,116 +219,121 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       const MV* sval = reinterpret_cast<const MV*>(base + col_b);
       const Raw* sold = reinterpret_cast<const Raw*>(base + col_b + val_b);
       const Raw* svl = reinterpret_cast<const Raw*>(base + col_b + val_b + vec_b);
-      const int64_t row0 = tile_of(k) * TILE;
-      typename AccOf<T, VPT>::type accum[U];
-      for (int s = 0; s < L; s += 4) {
-        int c[U][4];
-        MV h[U][4];
-        Cx<T, VPT> x[U][4];
+      {
+        const int rb = sb * TILE;  // this sub-tile's first row within the stage
+        const int64_t row0 = tile_of(k) * STILE + rb;
+        typename AccOf<T, VPT>::type accum[U];
+        for (int s = 0; s < L; s += 4) {
+          int c[U][4];
+          MV h[U][4];
+          Cx<T, VPT> x[U][4];
 #pragma unroll
-        for (int u = 0; u < U; ++u)
+          for (int u = 0; u < U; ++u)
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
-            if (s + j < L) {
-              c[u][j] = scol[(s + j) * TILE + u * RPB + rl];
-              h[u][j] = sval[(s + j) * TILE + u * RPB + rl];
+            for (int j = 0; j < 4; ++j)
+              if (s + j < L) {
+                c[u][j] = scol[(s + j) * STILE + rb + u * RPB + rl];
+                h[u][j] = sval[(s + j) * STILE + rb + u * RPB + rl];
+              }
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (s + j < L) unpack(__ldg(tcur + (int64_t)c[u][j] * TPR + sub), x[u][j]);
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            if (s == 0) {
+              Cx<T, VPT> old;
+              unpack(sold[(rb + u * RPB + rl) * TPR + sub], old);
+              madd_first_neg(accum[u], h[u][0], x[u][0], old);
+            } else {
+              madd(accum[u], h[u][0], x[u][0]);
             }
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-#pragma unroll
-          for (int j = 0; j < 4; ++j)
-            if (s + j < L) unpack(__ldg(tcur + (int64_t)c[u][j] * TPR + sub), x[u][j]);
+            for (int j = 1; j < 4; ++j)
+              if (s + j < L) madd(accum[u], h[u][j], x[u][j]);
+          }
+        }
+        Cx<T, VPT> acc[U], l[U];
+        T hvs[U][VPT];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          if (s == 0) {
-            Cx<T, VPT> old;
-            unpack(sold[(u * RPB + rl) * TPR + sub], old);
-            madd_first_neg(accum[u], h[u][0], x[u][0], old);
-          } else {
-            madd(accum[u], h[u][0], x[u][0]);
-          }
+          acc[u] = finish(accum[u]);
+          if (dbl) {
+            const T* shv = reinterpret_cast<const T*>(svl) + ((rb + u * RPB + rl) * TPR + sub) * VPT;
 #pragma unroll
-          for (int j = 1; j < 4; ++j)
-            if (s + j < L) madd(accum[u], h[u][j], x[u][j]);
+            for (int q = 0; q < VPT; ++q) hvs[u][q] = shv[q];
+          } else if (mom || ser) {
+            unpack(svl[(rb + u * RPB + rl) * TPR + sub], l[u]);
+          }
         }
-      }
-      Cx<T, VPT> acc[U], l[U];
-      T hvs[U][VPT];
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        acc[u] = finish(accum[u]);
-        if (dbl) {
-          const T* shv = reinterpret_cast<const T*>(svl) + ((u * RPB + rl) * TPR + sub) * VPT;
-#pragma unroll
-          for (int q = 0; q < VPT; ++q) hvs[u][q] = shv[q];
-        } else if (mom || ser) {
-          unpack(svl[(u * RPB + rl) * TPR + sub], l[u]);
+        // after its last sub-tile the stage is no longer read: hand it back to the producer
+        if (sb == SB - 1) {
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&empty[st]);
         }
-      }
-      // the stage is no longer read: hand it back to the producer
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[st]);
 #pragma unroll
-      for (int u = 0; u < U; ++u) {
-        const int64_t vi = (row0 + u * RPB + rl) * TPR + sub;
-        tout[vi] = pack(acc[u]);
-        if (ser) {
-          Cx<T, VPT> o;
+        for (int u = 0; u < U; ++u) {
+          const int64_t vi = (row0 + u * RPB + rl) * TPR + sub;
+          tout[vi] = pack(acc[u]);
+          if (ser) {
+            Cx<T, VPT> o;
 #pragma unroll
-          for (int q = 0; q < VPT; ++q) {
-            // y = c_m*x + 1*y, the expression of the grid-stride kernel (two nested FMAs)
-            o.re[q] = fma((T)cm.x, acc[u].re[q], fma(-(T)cm.y, acc[u].im[q], l[u].re[q]));
-            o.im[q] = fma((T)cm.x, acc[u].im[q], fma((T)cm.y, acc[u].re[q], l[u].im[q]));
+            for (int q = 0; q < VPT; ++q) {
+              // y = c_m*x + 1*y, the expression of the grid-stride kernel (two nested FMAs)
+              o.re[q] = fma((T)cm.x, acc[u].re[q], fma(-(T)cm.y, acc[u].im[q], l[u].re[q]));
+              o.im[q] = fma((T)cm.x, acc[u].im[q], fma((T)cm.y, acc[u].re[q], l[u].im[q]));
+            }
+            series[vi] = pack(o);
+            continue;
           }
-          series[vi] = pack(o);
-          continue;
-        }
-        if (!mom) continue;
-        if constexpr (FFM) {
-          const FF lf = ff_from_slot(l[u].re[0], l[u].im[0]);
-          FF tf;
-          bool ok = ff_split_f64(acc[u].re[0], tf.rh, tf.rl);
-          ok &= ff_split_f64(acc[u].im[0], tf.ih, tf.il);
-          ok &= ff_left_ok(lf.rh) & ff_left_ok(lf.ih);
-          if (ok) {
-            ff_cdot(fm, lf, tf);
-          } else {
-            const double2 lv = __ldg(vl64 + vi);
-            cdot_acc(mr[0], mi[0], lv.x, lv.y, acc[u].re[0], acc[u].im[0]);
-          }
-          if (++ffp == kFfFoldRows) {
-            ffp = 0;
-            ff_fold(mr[0], mi[0], fm);
-          }
-        } else if (dbl) {
-          Cx<T, VPT> own;  // T_m at this row
-          unpack(__ldg(tcur + vi), own);
-#pragma unroll
-          for (int q = 0; q < VPT; ++q) {
-            if (F32) {
-              cdot_acc(fr[q], fi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
-              fr2[q] += fmaf(own.re[q], own.re[q], fmaf(own.im[q], own.im[q], -hvs[u][q]));
+          if (!mom) continue;
+          if constexpr (FFM) {
+            const FF lf = ff_from_slot(l[u].re[0], l[u].im[0]);
+            FF tf;
+            bool ok = ff_split_f64(acc[u].re[0], tf.rh, tf.rl);
+            ok &= ff_split_f64(acc[u].im[0], tf.ih, tf.il);
+            ok &= ff_left_ok(lf.rh) & ff_left_ok(lf.ih);
+            if (ok) {
+              ff_cdot(fm, lf, tf);
             } else {
-              cdot_acc(mr[q], mi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
-              mr2[q] += fma(own.re[q], own.re[q], fma(own.im[q], own.im[q], -hvs[u][q]));
+              const double2 lv = __ldg(vl64 + vi);
+              cdot_acc(mr[0], mi[0], lv.x, lv.y, acc[u].re[0], acc[u].im[0]);
+            }
+            if (++ffp == kFfFoldRows) {
+              ffp = 0;
+              ff_fold(mr[0], mi[0], fm);
+            }
+          } else if (dbl) {
+            Cx<T, VPT> own;  // T_m at this row
+            unpack(__ldg(tcur + vi), own);
+#pragma unroll
+            for (int q = 0; q < VPT; ++q) {
+              if (F32) {
+                cdot_acc(fr[q], fi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
+                fr2[q] += fmaf(own.re[q], own.re[q], fmaf(own.im[q], own.im[q], -hvs[u][q]));
+              } else {
+                cdot_acc(mr[q], mi[q], acc[u].re[q], acc[u].im[q], own.re[q], own.im[q]);
+                mr2[q] += fma(own.re[q], own.re[q], fma(own.im[q], own.im[q], -hvs[u][q]));
+              }
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < VPT; ++q) {
+              if (F32)
+                cdot_acc(fr[q], fi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+              else
+                cdot_acc(mr[q], mi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
             }
           }
-        } else {
-#pragma unroll
-          for (int q = 0; q < VPT; ++q) {
-            if (F32)
-              cdot_acc(fr[q], fi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
-            else
-              cdot_acc(mr[q], mi[q], l[u].re[q], l[u].im[q], acc[u].re[q], acc[u].im[q]);
+          if (F32 && ++pending == kFlush) {
+            pending = 0;
+            fold();
           }
-        }
-        if (F32 && ++pending == kFlush) {
-          pending = 0;
-          fold();
         }
       }
     }
-    if (per_tile && mom) {
+    if (per_tile && mom && sb == SB - 1) {
       const int next_inst = (k + 1 < my_count) ? p.tile_inst[seg_tb + k + 1] : -1;
       if (next_inst != cur_inst) {
         if (F32) {
@@ -341,11 +353,11 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
   }
 }
 
-template <typename T, bool REAL, int TPR, int VPT, int U, int K>
+template <typename T, bool REAL, int TPR, int VPT, int U, int K, int SB>
 bool ws_smem_attr(size_t smem) {
   static size_t configured = 0;
   if (smem <= configured) return true;
-  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K>,
+  cudaError_t e = cudaFuncSetAttribute(cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K, SB>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -356,32 +368,37 @@ bool ws_smem_attr(size_t smem) {
   return true;
 }
 
-template <typename T, bool REAL, int TPR, int VPT, int U>
+// Shared memory of one instantiation: its stage count times a stage of SB sub-tiles.
+template <typename T, bool REAL, int TPR, int VPT, int U, int K, int SB>
+size_t ws_smem_bytes(int L) {
+  return ws_stages<T, REAL, TPR, U, K, SB>() * staged_stage_bytes<T, REAL, TPR, VPT, U * SB>(L, 2);
+}
+
+template <typename T, bool REAL, int TPR, int VPT, int U, int K, int SB>
+bool ws_go(const StepParams& p, int grid, cudaStream_t s) {
+  const size_t smem = ws_smem_bytes<T, REAL, TPR, VPT, U, K, SB>(p.L);
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U, K, SB>(smem)) return false;
+  cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K, SB><<<grid, kWsThreads, smem, s>>>(p);
+  return true;
+}
+
+template <typename T, bool REAL, int TPR, int VPT, int U, int SB>
 int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
-  const size_t stage = staged_stage_bytes<T, REAL, TPR, VPT, U>(p.L, 2);
-  const size_t smem = kWsStages * stage;
-  bool launched = false;
+  bool ok;
   if (p.dbl) {
-    if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsDbl>(smem)) return KPM_ERR_UNSUPPORTED;
-    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsDbl><<<grid, kWsThreads, smem, s>>>(p);
-    launched = true;
+    ok = ws_go<T, REAL, TPR, VPT, U, kWsDbl, SB>(p, grid, s);
   } else if (p.series && !p.vl) {
-    if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsSeries>(smem)) return KPM_ERR_UNSUPPORTED;
-    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsSeries><<<grid, kWsThreads, smem, s>>>(p);
-    launched = true;
-  }
-  if constexpr (sizeof(T) == 8 && VPT == 1) {
-    if (!launched && p.vl_ff && p.vl && !p.dbl) {
-      const size_t smem_ff = ws_stages<T, REAL, TPR, U, kWsFF>() * stage;
-      if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsFF>(smem_ff)) return KPM_ERR_UNSUPPORTED;
-      cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsFF><<<grid, kWsThreads, smem_ff, s>>>(p);
-      launched = true;
+    ok = ws_go<T, REAL, TPR, VPT, U, kWsSeries, SB>(p, grid, s);
+  } else {
+    bool ff = false;
+    if constexpr (sizeof(T) == 8 && VPT == 1) ff = p.vl_ff && p.vl;
+    if (ff) {
+      if constexpr (sizeof(T) == 8 && VPT == 1) ok = ws_go<T, REAL, TPR, VPT, U, kWsFF, SB>(p, grid, s);
+    } else {
+      ok = ws_go<T, REAL, TPR, VPT, U, kWsMom, SB>(p, grid, s);
     }
   }
-  if (!launched) {
-    if (!ws_smem_attr<T, REAL, TPR, VPT, U, kWsMom>(smem)) return KPM_ERR_UNSUPPORTED;
-    cheb_next_ws_kernel<T, REAL, TPR, VPT, U, kWsMom><<<grid, kWsThreads, smem, s>>>(p);
-  }
+  if (!ok) return KPM_ERR_UNSUPPORTED;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
@@ -391,13 +408,13 @@ int launch_ws(const StepParams& p, int grid, cudaStream_t s) {
 }
 
 // CTAs of one SM for epilogue variant K
-template <typename T, bool REAL, int TPR, int VPT, int U, int K>
-int ws_ctas_per_sm_k(int L, int nvec) {
-  const size_t smem = ws_stages<T, REAL, TPR, U, K>() * staged_stage_bytes<T, REAL, TPR, VPT, U>(L, nvec);
+template <typename T, bool REAL, int TPR, int VPT, int U, int K, int SB>
+int ws_ctas_per_sm_k(int L) {
+  const size_t smem = ws_smem_bytes<T, REAL, TPR, VPT, U, K, SB>(L);
   if (smem > 200 * 1024) return 0;
-  if (!ws_smem_attr<T, REAL, TPR, VPT, U, K>(smem)) return 0;
+  if (!ws_smem_attr<T, REAL, TPR, VPT, U, K, SB>(smem)) return 0;
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K>, kWsThreads,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, cheb_next_ws_kernel<T, REAL, TPR, VPT, U, K, SB>, kWsThreads,
                                                     smem) != cudaSuccess) {
     (void)cudaGetLastError();
     return 0;
@@ -408,60 +425,73 @@ int ws_ctas_per_sm_k(int L, int nvec) {
 // ff: the launches will be the float-float-products variant (its stage count and register
 // bound can differ); otherwise the moment variant, whose bound the series and doubled
 // variants share
-template <typename T, bool REAL, int TPR, int VPT, int U>
-int ws_ctas_per_sm(int L, int nvec, bool ff) {
+template <typename T, bool REAL, int TPR, int VPT, int U, int SB>
+int ws_ctas_per_sm(int L, bool ff) {
   if constexpr (sizeof(T) == 8 && VPT == 1) {
-    if (ff) return ws_ctas_per_sm_k<T, REAL, TPR, VPT, U, kWsFF>(L, nvec);
+    if (ff) return ws_ctas_per_sm_k<T, REAL, TPR, VPT, U, kWsFF, SB>(L);
   }
-  return ws_ctas_per_sm_k<T, REAL, TPR, VPT, U, kWsMom>(L, nvec);
+  return ws_ctas_per_sm_k<T, REAL, TPR, VPT, U, kWsMom, SB>(L);
 }
 
-// Dispatch over (real, R, U) for one precision (VPT as in the staged kernel).
+// Dispatch over (real, R, U, SB) for one precision (VPT as in the staged kernel).  SB = 2
+// (two sub-tiles per stage) exists for complex128, U = 1 and plain operators (the batched
+// per-tile tables count tiles of TILE rows).
 template <typename T>
 struct Ws {
-  template <bool REAL, int R, int U>
+  template <bool REAL, int R, int U, int SB>
   static int go(const StepParams& p, int grid, cudaStream_t s) {
     constexpr int VPT = (std::is_same<T, float>::value && R >= 2) ? 2 : 1;
-    return launch_ws<T, REAL, R / VPT, VPT, U>(p, grid, s);
+    return launch_ws<T, REAL, R / VPT, VPT, U, SB>(p, grid, s);
   }
-  template <bool REAL, int R, int U>
-  static int occ(int L, int nvec, bool ff) {
+  template <bool REAL, int R, int U, int SB>
+  static int occ(int L, bool ff) {
     constexpr int VPT = (std::is_same<T, float>::value && R >= 2) ? 2 : 1;
-    return ws_ctas_per_sm<T, REAL, R / VPT, VPT, U>(L, nvec, ff);
+    return ws_ctas_per_sm<T, REAL, R / VPT, VPT, U, SB>(L, ff);
   }
   template <bool REAL, int R>
-  static int go_u(int U, const StepParams& p, int grid, cudaStream_t s) {
-    return U == 2 ? go<REAL, R, 2>(p, grid, s) : go<REAL, R, 1>(p, grid, s);
+  static int go_u(int U, int SB, const StepParams& p, int grid, cudaStream_t s) {
+    if constexpr (sizeof(T) == 8) {
+      if (SB == 2 && U == 1) {
+        if (p.per_tile) return KPM_ERR_UNSUPPORTED;
+        return go<REAL, R, 1, 2>(p, grid, s);
+      }
+    }
+    if (SB != 1) return KPM_ERR_UNSUPPORTED;
+    return U == 2 ? go<REAL, R, 2, 1>(p, grid, s) : go<REAL, R, 1, 1>(p, grid, s);
   }
   template <bool REAL, int R>
-  static int occ_u(int U, int L, int nvec, bool ff) {
-    return U == 2 ? occ<REAL, R, 2>(L, nvec, ff) : occ<REAL, R, 1>(L, nvec, ff);
+  static int occ_u(int U, int SB, int L, bool ff) {
+    if constexpr (sizeof(T) == 8) {
+      if (SB == 2 && U == 1) return occ<REAL, R, 1, 2>(L, ff);
+    }
+    if (SB != 1) return 0;
+    return U == 2 ? occ<REAL, R, 2, 1>(L, ff) : occ<REAL, R, 1, 1>(L, ff);
   }
   template <bool REAL>
-  static int go_r(int R, int U, const StepParams& p, int grid, cudaStream_t s) {
+  static int go_r(int R, int U, int SB, const StepParams& p, int grid, cudaStream_t s) {
     switch (R) {
-      case 1: return go_u<REAL, 1>(U, p, grid, s);
-      case 2: return go_u<REAL, 2>(U, p, grid, s);
-      case 4: return go_u<REAL, 4>(U, p, grid, s);
-      case 8: return go_u<REAL, 8>(U, p, grid, s);
+      case 1: return go_u<REAL, 1>(U, SB, p, grid, s);
+      case 2: return go_u<REAL, 2>(U, SB, p, grid, s);
+      case 4: return go_u<REAL, 4>(U, SB, p, grid, s);
+      case 8: return go_u<REAL, 8>(U, SB, p, grid, s);
       default: return KPM_ERR_UNSUPPORTED;
     }
   }
   template <bool REAL>
-  static int occ_r(int R, int U, int L, int nvec, bool ff) {
+  static int occ_r(int R, int U, int SB, int L, bool ff) {
     switch (R) {
-      case 1: return occ_u<REAL, 1>(U, L, nvec, ff);
-      case 2: return occ_u<REAL, 2>(U, L, nvec, ff);
-      case 4: return occ_u<REAL, 4>(U, L, nvec, ff);
-      case 8: return occ_u<REAL, 8>(U, L, nvec, ff);
+      case 1: return occ_u<REAL, 1>(U, SB, L, ff);
+      case 2: return occ_u<REAL, 2>(U, SB, L, ff);
+      case 4: return occ_u<REAL, 4>(U, SB, L, ff);
+      case 8: return occ_u<REAL, 8>(U, SB, L, ff);
       default: return 0;
     }
   }
-  static int launch(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s) {
-    return real ? go_r<true>(R, U, p, grid, s) : go_r<false>(R, U, p, grid, s);
+  static int launch(bool real, int R, int U, const StepParams& p, int grid, cudaStream_t s, int SB = 1) {
+    return real ? go_r<true>(R, U, SB, p, grid, s) : go_r<false>(R, U, SB, p, grid, s);
   }
-  static int ctas_per_sm(bool real, int R, int U, int L, int nvec, bool ff = false) {
-    return real ? occ_r<true>(R, U, L, nvec, ff) : occ_r<false>(R, U, L, nvec, ff);
+  static int ctas_per_sm(bool real, int R, int U, int L, bool ff = false, int SB = 1) {
+    return real ? occ_r<true>(R, U, SB, L, ff) : occ_r<false>(R, U, SB, L, ff);
   }
 };
 

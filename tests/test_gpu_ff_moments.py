@@ -40,7 +40,7 @@ def _moments(monkeypatch, Hk, vs, M, kernel, fp64, v_l=None):
     return np.asarray(device.cheb_moments(op, M, vs, v_l=v_l))
 
 
-@pytest.mark.parametrize("kernel", ["ws1", "ws2"])
+@pytest.mark.parametrize("kernel", ["ws1", "ws2", "ws1s2"])
 @pytest.mark.parametrize("complex_hops", [False, True])
 @pytest.mark.parametrize("R", [1, 3, 8])
 def test_ff_products_against_oracle_and_fp64(cuda_lib, monkeypatch, kernel, complex_hops, R):

@@ -222,7 +222,7 @@ def test_long_recursion_crosses_moment_chunks(cuda_lib):
 
 
 @pytest.mark.parametrize("doubled", [False, True])
-@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2", "ws1", "ws2"])
+@pytest.mark.parametrize("kernel", ["simple", "staged1", "staged2", "ws1", "ws2", "ws1s2"])
 @pytest.mark.parametrize("dtype,R", [("c128", 8), ("c128", 1), ("c128", 4), ("c64", 2), ("c64", 8), ("c64", 1)])
 def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R, doubled):
     """Each recursion-step kernel the autotuner can pick, forced, against the oracle
@@ -230,6 +230,8 @@ def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R, doub
     and for doubled moments (which the staged kernels do not serve)."""
     if doubled and kernel.startswith("staged"):
         pytest.skip("doubled moments run on the grid-stride and producer-warp kernels")
+    if kernel == "ws1s2" and dtype == "c64":
+        pytest.skip("two sub-tiles per stage is a complex128 form")
     from minijclsquant_gb300 import _capi, device, lattice
     from minijclsquant_gb300.modifiers import modifier_bounds
     from minijclsquant_gb300.observables import random_vector_generator
@@ -246,7 +248,7 @@ def test_every_step_kernel_variant(cuda_lib, monkeypatch, kernel, dtype, R, doub
     code = _capi.KPM_C128 if dtype == "c128" else _capi.KPM_C64
     assert cuda_lib.kpm_ell_step_config(op.handle, code, R, ctypes.byref(kind), ctypes.byref(U), None, None) == 0
     assert (kind.value, U.value) == {"simple": (0, 1), "staged1": (1, 1), "staged2": (1, 2), "ws1": (2, 1),
-                                     "ws2": (2, 2)}[kernel]
+                                     "ws2": (2, 2), "ws1s2": (3, 1)}[kernel]
     assert cuda_lib.kpm_ell_check(op.handle, None) == 0
     for r in range(R):
         ref = oracle.rec_A_tab(150, Hk.data, Hk.indices, Hk.len_row, vs[r])

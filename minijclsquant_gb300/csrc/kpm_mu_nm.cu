@@ -100,6 +100,51 @@ __device__ __forceinline__ int chunk_kc(int c) { return (c >> 3) & 3; }
 __device__ __forceinline__ float4 tf32x4(float4 x) {
   return make_float4(to_tf32(x.x), to_tf32(x.y), to_tf32(x.z), to_tf32(x.w));
 }
+// The TMA-fed kernels round with integer operations (two per element instead of the
+// compiler's sequence for cvt.rna.tf32); the thread-loaded kernel keeps cvt.rna, so the
+// bit-for-bit agreement of the two forms also checks the rounding.
+__device__ __forceinline__ float4 tf32x4_int(float4 x) {
+  return make_float4(to_tf32_int(x.x), to_tf32_int(x.y), to_tf32_int(x.z), to_tf32_int(x.w));
+}
+
+// One thread's split of a raw A chunk and a raw B chunk of a K tile into the stage: hi and lo
+// of A, and of B both as it is (rows 0..127 of BX) and pairwise swapped with the new
+// imaginary part negated (rows 128..255).
+__device__ __forceinline__ void split_chunks(const unsigned char* rw, unsigned char* stage, uint32_t off,
+                                             uint32_t offs) {
+  {
+    const float4 x = *reinterpret_cast<const float4*>(rw + off);
+    const float4 hi = tf32x4_int(x);
+    const float4 lo = tf32x4_int(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
+    *reinterpret_cast<float4*>(stage + off) = hi;
+    *reinterpret_cast<float4*>(stage + kTileA + off) = lo;
+  }
+  {
+    const float4 x = *reinterpret_cast<const float4*>(rw + kTileA + off);
+    const float4 hi = tf32x4_int(x);
+    const float4 lo = tf32x4_int(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
+    unsigned char* bx = stage + 2 * kTileA;
+    *reinterpret_cast<float4*>(bx + off) = hi;
+    *reinterpret_cast<float4*>(bx + kTileBX + off) = lo;
+    *reinterpret_cast<float4*>(bx + offs) = make_float4(hi.y, -hi.x, hi.w, -hi.z);
+    *reinterpret_cast<float4*>(bx + kTileBX + offs) = make_float4(lo.y, -lo.x, lo.w, -lo.z);
+  }
+}
+
+// Adds chain buffer columns [base, base + kColsPerThread) of this thread's TMEM lane into
+// run[] with packed pairwise adds (one 16-column load per wait: a second one in flight
+// would spill at this kernel's 128 registers).
+__device__ __forceinline__ void fold_tmem(uint32_t base, float (&run)[kColsPerThread]) {
+#pragma unroll
+  for (int g = 0; g < kColsPerThread / 16; ++g) {
+    uint32_t a[16];
+    tmem_ld16_nowait(base + (uint32_t)(g * 16), a);
+    tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 16; i += 2)
+      add_f32x2(run[g * 16 + i], run[g * 16 + i + 1], __uint_as_float(a[i]), __uint_as_float(a[i + 1]));
+  }
+}
 
 // Adds a thread's level-1 sums run[] (one TMEM lane, kColsPerThread columns; column c at
 // ohi[c * kTile]) into its float-float partial (TwoSum into hi, the rounding error into lo)
@@ -342,6 +387,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) mu_gemm_kernel(const GemmPara
 // writes its hi / lo / swapped chunks at the same offsets, free of bank conflicts.
 // Accumulation, chains, folds and partials are those of mu_gemm_kernel.
 constexpr int kRawStages = 4;
+static_assert((kRawStages & (kRawStages - 1)) == 0, "the raw ring index wraps with a mask");
 constexpr uint32_t kRawBytes = 2 * kTileA;                    // raw A and B tiles, 16 KB
 constexpr uint32_t kTmaSmem = kRawStages * kRawBytes + kGemmStages * kStageBytes;  // 208 KB
 
@@ -442,14 +488,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
     ok = __all_sync(0xffffffffu, ok);
     if (!ok) return false;
     tc_fence_after();
-    const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((c & 1) * 256 + cb);
-#pragma unroll
-    for (int g = 0; g < kColsPerThread / 16; ++g) {
-      float v[16];
-      tmem_ld16(base + (uint32_t)(g * 16), v);
-#pragma unroll
-      for (int i = 0; i < 16; ++i) run[g * 16 + i] = __fadd_rn(run[g * 16 + i], v[i]);
-    }
+    fold_tmem(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)((c & 1) * 256 + cb), run);
     return true;
   };
   auto flush_l2 = [&]() {
@@ -463,9 +502,13 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
   int issued = 0;  // K tiles whose MMAs thread 0 has issued
   int t = 0;
   bool ok = true;
+  // the split stage of tile t and the parity of its next wait advance with t (no division by
+  // three in the loop): bit s of sph is the parity of the next wait on split stage s; the raw
+  // ring has a power-of-two length
+  int st = 0;
+  uint32_t sph = 0;
   for (; t < k_tiles && ok; ++t) {
-    const int st = t % kGemmStages;
-    const int rs = t % kRawStages;
+    const int rs = t & (kRawStages - 1);
     const int c = t / kChainTiles;
     bool good = true;
     if (t % kChainTiles == 0 && c >= 2) {
@@ -475,30 +518,12 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         chains_in_l1 = 0;
       }
     }
-    if (good && t >= kGemmStages)
-      good = mbar_wait_bounded(&bars[st], (uint32_t)(((t - kGemmStages) / kGemmStages) & 1));
-    if (good) good = mbar_wait_bounded(&rawbar[rs], (uint32_t)((t / kRawStages) & 1));
-    if (good) {
-      const unsigned char* rw = raw + (size_t)rs * kRawBytes;
-      unsigned char* stage = split + (size_t)st * kStageBytes;
-      {
-        const float4 x = *reinterpret_cast<const float4*>(rw + off);
-        const float4 hi = tf32x4(x);
-        const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
-        *reinterpret_cast<float4*>(stage + off) = hi;
-        *reinterpret_cast<float4*>(stage + kTileA + off) = lo;
-      }
-      {
-        const float4 x = *reinterpret_cast<const float4*>(rw + kTileA + off);
-        const float4 hi = tf32x4(x);
-        const float4 lo = tf32x4(make_float4(x.x - hi.x, x.y - hi.y, x.z - hi.z, x.w - hi.w));
-        unsigned char* bx = stage + 2 * kTileA;
-        *reinterpret_cast<float4*>(bx + off) = hi;
-        *reinterpret_cast<float4*>(bx + kTileBX + off) = lo;
-        *reinterpret_cast<float4*>(bx + offs) = make_float4(hi.y, -hi.x, hi.w, -hi.z);
-        *reinterpret_cast<float4*>(bx + kTileBX + offs) = make_float4(lo.y, -lo.x, lo.w, -lo.z);
-      }
+    if (good && t >= kGemmStages) {
+      good = mbar_wait_bounded(&bars[st], (sph >> st) & 1u);
+      sph ^= 1u << st;
     }
+    if (good) good = mbar_wait_bounded(&rawbar[rs], (uint32_t)(t / kRawStages) & 1u);
+    if (good) split_chunks(raw + (size_t)rs * kRawBytes, split + (size_t)st * kStageBytes, off, offs);
     fence_proxy_async_shared();
     tc_fence_before();
     if (__syncthreads_or(!good)) {
@@ -530,6 +555,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1)
         ++raw_issued;
       }
     }
+    st = st == kGemmStages - 1 ? 0 : st + 1;
   }
   if (ok) {
     const int nchains = (k_tiles + kChainTiles - 1) / kChainTiles;
@@ -672,7 +698,7 @@ int mu_contract(const float* A, const float* B, int64_t K, int64_t lda, int Nm, 
              : (operand_map(&ma, A, lda, mt * kTile) && operand_map(&mb, B, lda, mt * kTile));
   g_last_gemm_tma = (tma ? 1 : 0) + (sw ? 2 : 0);
   static bool attr[4] = {false, false, false, false};
-  const int which = (tma ? 1 : 0) + (sw ? 2 : 0);
+  const int which = g_last_gemm_tma;
   if (!attr[which]) {
     const void* fn = tma ? (sw ? (const void*)mu_gemm_tma_kernel<true> : (const void*)mu_gemm_tma_kernel<false>)
                          : (sw ? (const void*)mu_gemm_kernel<true> : (const void*)mu_gemm_kernel<false>);

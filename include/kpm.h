@@ -425,6 +425,11 @@ int kpm_phonon_modifier(int64_t n, int len_row, const double* params, const doub
  * where std::complex<double>* is passed as double* (identical layout).
  * Host buffers in and out; synchronous; the operator is uploaded per call,
  * as in the reference.  Status: kpm_last_status() (per host thread).
+ * rec_A_tab and rec_A_tab_2 keep one operator's device arrays and buffers
+ * allocated between calls of the same shape on the same device (the values are
+ * still uploaded, validated and repacked every call), so a loop over vectors
+ * allocates device memory once; a call made while another thread is in one
+ * uses buffers of its own.
  * for_time updates U and U_c in place (len_t <= 0 leaves them unchanged, as the
  * reference's loop does).
  */
@@ -437,6 +442,9 @@ void for_time_sigma(double* data, double* data2, double* data3, int* indices, in
                     double* moments_kernel_U, double* moments_kernel_FD, int len_t,
                     double* sigma_vec, double* v, int M, int M2);
 int kpm_last_status(void);
+/* Frees the device memory rec_A_tab / rec_A_tab_2 keep between calls (no
+ * counterpart in the reference, whose wrappers allocate per call). */
+int kpm_host_cache_release(void);
 
 /* ---- measurement hooks (no counterpart in the reference) ----------------
  * kpm_ell_profile(h, 1) starts recording CUDA events around every recursion

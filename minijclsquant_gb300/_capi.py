@@ -60,6 +60,7 @@ SIGNATURES = {
     "kpm_cheb_commutator_table": (_I, [_P, _P, _I, _I, _I, _P, _P, _P, _P]),
     "kpm_time_sigma": (_I, [_P, _P, _P, _I, _I, _P, _I, _P, _I, _I, _P, _P, _P]),
     "rec_A_tab": (None, [_P, _P, _I, _I, _P, _P, _I]),
+    "kpm_host_cache_release": (_I, []),
     "rec_A_tab_2": (None, [_P, _P, _I, _I, _P, _P, _P, _I]),
     "for_time": (None, [_P, _P, _I, _I, _P, _I, _P, _P, _I]),
     "for_time_sigma": (None, [_P, _P, _P, _P, _I, _I, _P, _P, _I, _P, _P, _I, _I]),

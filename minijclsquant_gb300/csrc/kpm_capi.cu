@@ -735,14 +735,13 @@ const char* kpm_strerror(int status) {
 
 int kpm_version(void) { return 100; }
 
-int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* data, const int32_t* indices,
-                   unsigned flags, void* stream) {
-  if (!out || !data || !indices || n_rows < 1 || len_row < 1) return KPM_ERR_INVALID_ARG;
-  if (n_rows > (int64_t)INT32_MAX) return KPM_ERR_SHAPE;
-  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG | KPM_FLAG_DOUBLING | KPM_FLAG_COMPLEX))
-    return KPM_ERR_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+// A handle without values: shape, padding, device (the values come from load_operator).
+int new_handle(int64_t n_rows, int len_row, kpm_ell_s** out) {
   *out = nullptr;
-  cudaStream_t s = as_stream(stream);
   kpm_ell_s* h = new kpm_ell_s();
   static std::atomic<uint64_t> next_id{1};
   h->id = next_id.fetch_add(1);
@@ -758,37 +757,38 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
     return KPM_ERR_CUDA;
   }
   h->device = dev;
+  *out = h;
+  return KPM_OK;
+}
+
+// Upload (host pointers) or read (KPM_FLAG_DEVICE_PTRS) the reference-layout ELL arrays,
+// validate them on the device (indices, finiteness, real or complex, column fingerprint) and
+// repack them into h's SoA arrays, allocating those only when h has none of the right size.
+// stage_data / stage_idx / flag_buf are the caller's staging buffers (kept or released by
+// the caller).  Synchronises s.
+int load_operator(kpm_ell_s* h, const double* data, const int32_t* indices, unsigned flags, cudaStream_t s,
+                  DevBuf& stage_data, DevBuf& stage_idx, DevBuf& flag_buf) {
+  const int64_t n_rows = h->n;
+  const int len_row = h->L;
   const int64_t count = n_rows * (int64_t)len_row;
   const double2* d_data = reinterpret_cast<const double2*>(data);
   const int32_t* d_idx = indices;
-  DevBuf stage_data, stage_idx, flag_buf;
-  int st = KPM_OK;
-  auto fail = [&](int code) {
-    release(stage_data);
-    release(stage_idx);
-    release(flag_buf);
-    kpm_ell_destroy(h);
-    return code;
-  };
+  cudaError_t e = cudaSuccess;
   if (!(flags & KPM_FLAG_DEVICE_PTRS)) {
-    if ((st = ensure(stage_data, count * sizeof(double2))) != KPM_OK) return fail(st);
-    if ((st = ensure(stage_idx, count * sizeof(int32_t))) != KPM_OK) return fail(st);
+    KPM_TRY(ensure(stage_data, count * sizeof(double2)));
+    KPM_TRY(ensure(stage_idx, count * sizeof(int32_t)));
     e = cudaMemcpyAsync(stage_data.p, data, count * sizeof(double2), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess)
       e = cudaMemcpyAsync(stage_idx.p, indices, count * sizeof(int32_t), cudaMemcpyHostToDevice, s);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
-      return fail(KPM_ERR_CUDA);
+      return KPM_ERR_CUDA;
     }
     d_data = static_cast<const double2*>(stage_data.p);
     d_idx = static_cast<const int32_t*>(stage_idx.p);
   }
-  if ((st = ensure(flag_buf, 2 * sizeof(unsigned long long))) != KPM_OK) return fail(st);
-  e = cudaMemsetAsync(flag_buf.p, 0, 2 * sizeof(unsigned long long), s);
-  if (e != cudaSuccess) {
-    set_last_cuda_error(e);
-    return fail(KPM_ERR_CUDA);
-  }
+  KPM_TRY(ensure(flag_buf, 2 * sizeof(unsigned long long)));
+  KPM_CUDA_TRY(cudaMemsetAsync(flag_buf.p, 0, 2 * sizeof(unsigned long long), s));
   ell_validate_kernel<<<grid_1d(count), 256, 0, s>>>(d_data, d_idx, count, n_rows, len_row,
                                                      static_cast<unsigned*>(flag_buf.p),
                                                      static_cast<unsigned long long*>(flag_buf.p) + 1);
@@ -798,37 +798,65 @@ int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* dat
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
-    return fail(KPM_ERR_CUDA);
+    return KPM_ERR_CUDA;
   }
   const unsigned hflags = static_cast<unsigned>(hbuf[0] & 0xffffffffull);
+  if (hflags & 1u) return KPM_ERR_INDEX;
+  if (hflags & 4u) return KPM_ERR_NONFINITE;
+  const int is_real = ((hflags & 2u) || (flags & KPM_FLAG_COMPLEX)) ? 0 : 1;
+  if (h->val64 && is_real != h->is_real) {  // the value width changes: a new array
+    cudaFree(h->val64);
+    h->val64 = nullptr;
+  }
+  h->is_real = is_real;
   h->structure = hbuf[1];
-  if (hflags & 1u) return fail(KPM_ERR_INDEX);
-  if (hflags & 4u) return fail(KPM_ERR_NONFINITE);
-  h->is_real = ((hflags & 2u) || (flags & KPM_FLAG_COMPLEX)) ? 0 : 1;
   const int64_t slots = (int64_t)len_row * h->n_pad;
-  e = cudaMalloc(&h->val64, slots * (h->is_real ? sizeof(double) : sizeof(double2)));
-  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->col), slots * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&h->err_flag), sizeof(int));
+  e = cudaSuccess;
+  if (!h->val64) e = cudaMalloc(&h->val64, slots * (h->is_real ? sizeof(double) : sizeof(double2)));
+  if (e == cudaSuccess && !h->col) e = cudaMalloc(reinterpret_cast<void**>(&h->col), slots * sizeof(int32_t));
+  if (e == cudaSuccess && !h->err_flag) e = cudaMalloc(reinterpret_cast<void**>(&h->err_flag), sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(h->err_flag, 0, sizeof(int), s);
   if (e != cudaSuccess) {
     set_last_cuda_error(e);
     (void)cudaGetLastError();
-    return fail(KPM_ERR_OOM);
+    return KPM_ERR_OOM;
   }
   ell_repack_kernel<<<grid_1d(slots), 256, 0, s>>>(d_data, d_idx, n_rows, h->n_pad, len_row, h->is_real != 0,
                                                     h->val64, h->col);
-  e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) {
-    set_last_cuda_error(e);
-    return fail(KPM_ERR_CUDA);
-  }
+  KPM_CUDA_TRY(cudaGetLastError());
+  KPM_CUDA_TRY(cudaStreamSynchronize(s));
+  return KPM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int kpm_ell_create(kpm_ell** out, int64_t n_rows, int len_row, const double* data, const int32_t* indices,
+                   unsigned flags, void* stream) {
+  if (!out || !data || !indices || n_rows < 1 || len_row < 1) return KPM_ERR_INVALID_ARG;
+  if (n_rows > (int64_t)INT32_MAX) return KPM_ERR_SHAPE;
+  if (flags & ~(unsigned)(KPM_FLAG_DEVICE_PTRS | KPM_FLAG_SPLIT_DIAG | KPM_FLAG_DOUBLING | KPM_FLAG_COMPLEX))
+    return KPM_ERR_INVALID_ARG;
+  *out = nullptr;
+  cudaStream_t s = as_stream(stream);
+  kpm_ell_s* h = nullptr;
+  KPM_TRY(new_handle(n_rows, len_row, &h));
+  DevBuf stage_data, stage_idx, flag_buf;
+  int st = load_operator(h, data, indices, flags, s, stage_data, stage_idx, flag_buf);
   release(stage_data);
   release(stage_idx);
   release(flag_buf);
+  if (st != KPM_OK) {
+    kpm_ell_destroy(h);
+    return st;
+  }
   h->doubling = (flags & KPM_FLAG_DOUBLING) ? 1 : 0;
   if (h->doubling) {
-    if ((st = check_hermitian(h, s)) != KPM_OK) return fail(st);
+    if ((st = check_hermitian(h, s)) != KPM_OK) {
+      kpm_ell_destroy(h);
+      return st;
+    }
   } else {
     h->herm_stale = 1;  // checked when doubling is switched on or the property is read
   }
@@ -1309,32 +1337,100 @@ int kpm_ell_set_doubling(kpm_ell* h, int on) {
 }
 
 // ---- reference-compatible host-pointer entry points -------------------------
+// The reference uploads the operator on every call (its wrappers allocate and free device
+// memory per call).  rec_A_tab / rec_A_tab_2 upload it on every call too, but into one cached
+// operator whose device arrays, staging buffers and vector buffers stay allocated between
+// calls of the same shape (rows, slots) on the same device, so a caller looping over random
+// vectors pays no cudaMalloc / cudaFree after the first call.  The values are re-read,
+// re-validated and repacked each call, so results do not depend on the cache; state derived
+// from the old values (complex64 copy, recorded graphs, Hermiticity) is dropped.  A call
+// made while another thread holds the cache uses an operator of its own.
+// kpm_host_cache_release() frees the cache.
+struct HostCache {
+  std::mutex mu;
+  kpm_ell_s* h = nullptr;
+  DevBuf stage_data, stage_idx, flags, dv, dl, dmu;
+};
+static HostCache g_host;
+
+static void host_cache_drop(HostCache& c) {
+  if (c.h) {
+    int cur = -1;
+    const bool other = cudaGetDevice(&cur) == cudaSuccess && cur != c.h->device;
+    if (other) (void)cudaSetDevice(c.h->device);
+    kpm_ell_destroy(c.h);
+    DevBuf* bufs[] = {&c.stage_data, &c.stage_idx, &c.flags, &c.dv, &c.dl, &c.dmu};
+    for (DevBuf* b : bufs) release(*b);
+    if (other) (void)cudaSetDevice(cur);
+  }
+  c.h = nullptr;
+}
+
+// Forget everything derived from the previous values of a cached operator.
+static void reset_derived(kpm_ell_s* h) {
+  if (h->val32) {
+    cudaFree(h->val32);
+    h->val32 = nullptr;
+  }
+  for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
+  h->graphs.clear();
+  h->tuned.clear();  // per-handle choices; the process-wide ones are keyed by shape and structure
+  h->hermitian = 0;
+  h->herm_stale = 1;
+  h->doubling = 0;
+  h->same_cols_id = 0;
+  h->adj_R = h->adj_M = h->adj_ckpt = 0;
+  static std::atomic<uint64_t> reload_id{1ull << 62};
+  h->id = reload_id.fetch_add(1);
+}
+
+static int host_moments(kpm_ell_s* h, DevBuf& dv, DevBuf& dl, DevBuf& dmu, int N, double* A_vec, double* v_l,
+                        double* v_r, int M) {
+  KPM_TRY(ensure(dv, (size_t)N * sizeof(double2)));
+  if (v_l) KPM_TRY(ensure(dl, (size_t)N * sizeof(double2)));
+  KPM_TRY(ensure(dmu, (size_t)M * sizeof(double2)));
+  KPM_CUDA_TRY(cudaMemcpy(dv.p, v_r, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice));
+  if (v_l) KPM_CUDA_TRY(cudaMemcpy(dl.p, v_l, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice));
+  KPM_TRY(kpm_cheb_moments(h, KPM_C128, 1, M, static_cast<double*>(dv.p), v_l ? static_cast<double*>(dl.p) : nullptr,
+                           static_cast<double*>(dmu.p), nullptr, nullptr));
+  KPM_CUDA_TRY(cudaMemcpy(A_vec, dmu.p, (size_t)M * sizeof(double2), cudaMemcpyDeviceToHost));
+  return KPM_OK;
+}
+
 static int host_rec(double* data, int* indices, int len_row, int N, double* A_vec, double* v_l, double* v_r,
                     int M) {
   if (!data || !indices || !A_vec || !v_r || N < 1 || len_row < 1 || M < 1) return KPM_ERR_INVALID_ARG;
-  kpm_ell* h = nullptr;
-  KPM_TRY(kpm_ell_create(&h, N, len_row, data, indices, 0u, nullptr));
-  DevBuf dv, dl, dmu;
-  int st = ensure(dv, (size_t)N * sizeof(double2));
-  if (st == KPM_OK && v_l) st = ensure(dl, (size_t)N * sizeof(double2));
-  if (st == KPM_OK) st = ensure(dmu, (size_t)M * sizeof(double2));
-  cudaError_t e = cudaSuccess;
-  if (st == KPM_OK) e = cudaMemcpy(dv.p, v_r, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice);
-  if (st == KPM_OK && e == cudaSuccess && v_l)
-    e = cudaMemcpy(dl.p, v_l, (size_t)N * sizeof(double2), cudaMemcpyHostToDevice);
-  if (st == KPM_OK && e == cudaSuccess)
-    st = kpm_cheb_moments(h, KPM_C128, 1, M, static_cast<double*>(dv.p), v_l ? static_cast<double*>(dl.p) : nullptr,
-                          static_cast<double*>(dmu.p), nullptr, nullptr);
-  if (st == KPM_OK && e == cudaSuccess) e = cudaMemcpy(A_vec, dmu.p, (size_t)M * sizeof(double2), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) {
-    set_last_cuda_error(e);
-    st = KPM_ERR_CUDA;
+  std::unique_lock<std::mutex> lock(g_host.mu, std::try_to_lock);
+  if (!lock.owns_lock()) {  // another thread is in a call: an operator of this call's own
+    kpm_ell* h = nullptr;
+    KPM_TRY(kpm_ell_create(&h, N, len_row, data, indices, 0u, nullptr));
+    DevBuf dv, dl, dmu;
+    const int st = host_moments(h, dv, dl, dmu, N, A_vec, v_l, v_r, M);
+    release(dv);
+    release(dl);
+    release(dmu);
+    kpm_ell_destroy(h);
+    return st;
   }
-  release(dv);
-  release(dl);
-  release(dmu);
-  kpm_ell_destroy(h);
+  int dev = 0;
+  KPM_CUDA_TRY(cudaGetDevice(&dev));
+  HostCache& c = g_host;
+  if (c.h && (c.h->device != dev || c.h->n != N || c.h->L != len_row)) host_cache_drop(c);
+  if (c.h) {
+    reset_derived(c.h);
+  } else {
+    KPM_TRY(new_handle(N, len_row, &c.h));
+  }
+  int st = load_operator(c.h, data, indices, 0u, nullptr, c.stage_data, c.stage_idx, c.flags);
+  if (st == KPM_OK) st = host_moments(c.h, c.dv, c.dl, c.dmu, N, A_vec, v_l, v_r, M);
+  if (st != KPM_OK) host_cache_drop(c);  // no half-loaded operator stays behind
   return st;
+}
+
+int kpm_host_cache_release(void) {
+  std::lock_guard<std::mutex> lock(g_host.mu);
+  host_cache_drop(g_host);
+  return KPM_OK;
 }
 
 void rec_A_tab(double* data, int* indices, int len_row, int N, double* A_vec, double* v, int M) {

@@ -56,11 +56,13 @@ constexpr int kWsDbl = 3;     // doubled moments (two sets per step)
 // real operator (three of its 20 KB stages per CTA let three CTAs share an SM), four otherwise.
 template <typename T, bool REAL, int TPR, int U, int K, int SB = 1>
 __host__ __device__ constexpr int ws_stages() {
+  // one-vector complex128 with two rows per thread: two 512-row stages, so two CTAs share an SM
+  if (sizeof(T) == 8 && REAL && TPR == 1 && U == 2) return 2;
   return ((sizeof(T) == 8 && REAL && TPR == 1 && U == 1 && K == kWsFF) || SB > 1) ? 3 : kWsStages;
 }
 
 template <typename T, bool REAL, int TPR, int VPT, int U, int K, int SB = 1>
-__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : ((sizeof(T) == 8 && REAL && TPR >= 2) ? 2 : 1)))
+__global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL && (TPR >= 2 || K == kWsFF)) ? 3 : 2) : ((sizeof(T) == 8 && REAL) ? 2 : 1)))
     cheb_next_ws_kernel(const StepParams p) {
   using Raw = typename RawT<T, VPT>::type;
   using MV = typename MatV<T, REAL>::type;

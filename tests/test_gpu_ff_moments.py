@@ -98,3 +98,24 @@ def test_ff_products_out_of_range_elements(cuda_lib, monkeypatch, case):
     ref = oracle.rec_A_tab(M, Hk.data, Hk.indices, Hk.len_row, v)
     ok, err = oracle.moment_tolerance_ok(mu, ref, REL)
     assert ok, (case, err)
+
+
+@pytest.mark.parametrize("kernel", ["simple", "staged1", "ws1", "ws2", "ws1s2"])
+@pytest.mark.parametrize("fp64", [False, True])
+def test_step_forms_are_deterministic(cuda_lib, monkeypatch, kernel, fp64):
+    """Each step form the autotuner can pick gives bit-identical moments when called twice on the same
+    inputs (every partial sum has a fixed place and order), at a size with several hundred tiles per
+    launch, so rounding differences between runs can only come from a change of form, never from
+    the run itself."""
+    from minijclsquant_gb300 import lattice
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    Hk = lattice.honeycomb(192, 160, t=-2.7, W=0.7, seed=9).modifier(modifier_bounds)
+    n = Hk.data.size // Hk.len_row
+    vs = np.stack([random_vector_generator(n, 90 + r) for r in range(8)])
+    a = _moments(monkeypatch, Hk, vs, 96, kernel, fp64)
+    b = _moments(monkeypatch, Hk, vs, 96, kernel, fp64)
+    assert np.array_equal(a, b), kernel
+    ref = oracle.rec_A_tab(96, Hk.data, Hk.indices, Hk.len_row, vs[0])
+    assert oracle.moment_tolerance_ok(a[0], ref, REL)[0]

@@ -179,6 +179,45 @@ def test_reference_compatible_host_entry_points(cuda_lib):
     assert np.max(np.abs(sig - x["sigma"])) <= REL * np.max(np.abs(x["sigma"]))
 
 
+def test_host_entry_point_reuses_its_operator_across_calls(cuda_lib):
+    """rec_A_tab keeps one operator's device arrays between calls of the same shape and reloads
+    the values every call: consecutive calls with different operators of one shape (real, then
+    complex hoppings, then real again, then the same values twice), a call of another shape, and
+    a call after kpm_host_cache_release each match the oracle; rec_A_tab_2 shares the cache."""
+    from minijclsquant_gb300 import lattice, obv_gpu
+    from minijclsquant_gb300.modifiers import modifier_bounds
+    from minijclsquant_gb300.observables import random_vector_generator
+
+    def op(nx, ny, seed, phase):
+        arr = lattice.honeycomb_arrays(nx, ny, t=-2.7, W=0.7, seed=seed)
+        if phase:
+            ph = np.exp(1j * phase * np.real(arr["dx"]) / 0.142)
+            arr = dict(arr, data=np.where(np.real(arr["dx"]) != 0, arr["data"] * ph, arr["data"]))
+        from minijclsquant_gb300.ell_matrix import ell_matrix
+
+        return ell_matrix(lattice.to_csr(arr)).modifier(modifier_bounds)
+
+    M = 80
+    cases = [op(24, 20, 1, 0.0), op(24, 20, 2, 0.3), op(24, 20, 3, 0.0), op(24, 20, 3, 0.0), op(30, 18, 4, 0.2)]
+    for k, Hk in enumerate(cases + cases[:2]):
+        if k == len(cases):
+            assert cuda_lib.kpm_host_cache_release() == 0
+        n = Hk.data.size // Hk.len_row
+        v = random_vector_generator(n, 600 + k)
+        out = np.zeros(M, dtype=np.complex128)
+        data = np.ascontiguousarray(Hk.data, dtype=np.complex128)
+        idx = np.ascontiguousarray(Hk.indices, dtype=np.int32)
+        obv_gpu.rec_A_tab_gpu(data, idx, Hk.len_row, v, out, M)
+        ref = oracle.rec_A_tab(M, Hk.data, Hk.indices, Hk.len_row, v)
+        assert oracle.moment_tolerance_ok(out, ref, REL)[0], k
+        vl = random_vector_generator(n, 700 + k)
+        out2 = np.zeros(M, dtype=np.complex128)
+        obv_gpu.rec_A_tab_2_gpu(data, idx, Hk.len_row, vl, v, out2, M)
+        ref2 = oracle.rec_A_tab2v(M, Hk.data, Hk.indices, Hk.len_row, vl, v)
+        assert oracle.moment_tolerance_ok(out2, ref2, REL)[0], k
+    assert cuda_lib.kpm_host_cache_release() == 0
+
+
 def test_ell_dot_matches_oracle(cuda_lib):
     from minijclsquant_gb300.ell_matrix import ell_matrix
 

@@ -45,6 +45,7 @@ struct TileCopy {
   const unsigned char* old;
   const unsigned char* vl;
   const unsigned char* vl2;
+  const unsigned char* cur;  // T_m: its rows of the tile are prefetched into L2 (null: none)
   int64_t ld;
   int L;
   uint32_t col_slab;   // bytes of one column slab (TILE * 4)
@@ -66,6 +67,8 @@ static __device__ __noinline__ void issue_tile(const TileCopy& tc, unsigned char
     bulk_g2s(stage + tc.col_b + (size_t)s * tc.val_slab, tc.val + ((int64_t)s * tc.ld + row0) * vbytes, tc.val_slab,
              bar, pol);
   const int64_t voff = row0 * vec_bytes_per_row;
+  // the tile's own rows of T_m, which its neighbour gathers touch first, into L2 ahead of them
+  if (tc.cur) bulk_prefetch_l2(tc.cur + voff, tc.vec_slab);
   bulk_g2s(stage + tc.col_b + tc.val_b, tc.old + voff, tc.vec_slab, bar, pol);
   if (tc.vl)
     bulk_g2s(stage + tc.col_b + tc.val_b + tc.vec_slab, tc.vl + row0 * (int64_t)(tc.vl_slab / tile), tc.vl_slab, bar,
@@ -121,6 +124,7 @@ __global__ void __launch_bounds__(kBlock, (U == 1 ? 3 : 2)) cheb_next_staged_ker
     tc.old = static_cast<const unsigned char*>(p.tout);
     tc.vl = static_cast<const unsigned char*>(p.vl);
     tc.vl2 = nullptr;
+    tc.cur = nullptr;
     tc.ld = p.ld;
     tc.L = L;
     tc.col_slab = TILE * 4;

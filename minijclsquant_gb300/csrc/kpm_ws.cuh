@@ -121,9 +121,10 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       // a series step (no moments) stages the series accumulator in the left-vector slot
       tc.vl = static_cast<const unsigned char*>(SER ? p.series : p.vl);
       tc.vl2 = nullptr;
-      // T_m's rows of each staged tile are prefetched into L2 (1.096 -> 1.063 ms per default step
-      // at 2048^2, R = 8): the neighbour gathers of the tile find them there
-      tc.cur = static_cast<const unsigned char*>(p.tcur);
+      // complex128: T_m's rows of each staged tile are prefetched into L2 (1.096 -> 1.063 ms per
+      // default step at 2048^2, R = 8), where the tile's neighbour gathers find them; the
+      // complex64 steps measured slower with it (batched ensemble 978 -> 1001 ms)
+      tc.cur = sizeof(T) == 8 ? static_cast<const unsigned char*>(p.tcur) : nullptr;
       tc.ld = p.ld;
       tc.L = L;
       tc.col_slab = STILE * 4;

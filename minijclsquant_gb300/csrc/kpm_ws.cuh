@@ -9,7 +9,13 @@
 // and an "empty" mbarrier (one arrival per compute warp once it has read the stage).  Compute warps never meet at a
 // CTA-wide barrier inside the tile loop, so while one warp waits on its
 // neighbour gathers T_m[col] the others compute, and the producer refills a
-// stage as soon as the last warp has left it.
+// stage as soon as the last warp has left it.  For complex128 the producer also
+// prefetches the tile's own rows of T_m into L2 when it stages the tile, so the
+// gathers, which touch those rows first, find them there.
+//
+// SB > 1 (complex128): a stage holds SB sub-tiles of TILE rows, taken by the compute
+// warps one after the other (the stage's wait comes with the first, its release with
+// the last), so each bulk copy brings SB times the rows at the registers of SB = 1.
 //
 // The series instantiation (K = kWsSeries) is a series step of rec_A_vec (p.series
 // set, p.vl null, no doubling): the producer stages the series accumulator tile in

@@ -703,7 +703,7 @@ int ff_corr_launch(bool rv, int R, const kpm_ell_s* v1, const float4* u, const f
 
 // Left vectors for float-float moment products of the FP64 recursion: complex128 [R][n] ->
 // float pairs [n_pad][Rg] (hi = the nearest float, lo = the nearest float to the rest).  A
-// component that is neither zero nor in [2^-50, 2^61) gets a NaN high part, which sends
+// component that is neither zero nor in [2^-50, 2^59) gets a NaN high part, which sends
 // that element to the FP64 product (ff_left_ok).
 __global__ void pack_left_ff_kernel(const double2* __restrict__ src, int64_t n, int64_t n_pad, int R, int r0, int Rg,
                                     float4* __restrict__ dst) {
@@ -718,7 +718,7 @@ __global__ void pack_left_ff_kernel(const double2* __restrict__ src, int64_t n, 
 #pragma unroll
     for (int k = 0; k < 2; ++k) {
       const double a = fabs(c[k]);
-      if (c[k] == 0.0 || (a >= 0x1p-50 && a < 0x1p61)) {
+      if (c[k] == 0.0 || (a >= 0x1p-50 && a < 0x1p59)) {
         q[k] = (float)c[k];
         q[k + 2] = (float)(c[k] - (double)q[k]);
       } else {

@@ -81,11 +81,12 @@ __device__ __forceinline__ void ff_fold(double& re, double& im, FFMom& m) {
 // when it must), lo = x - hi exactly as a signed 29-bit count of x's last-place units,
 // rounded to a float, so hi + lo = x to 2^-49 relative.  The left vector is packed once
 // per call (pack_left_ff).  Products run through ff_cdot, and the float-pair sums are
-// folded into FP64 every kFfFoldRows rows.  A value outside [2^-50, 2^61) that is not zero
+// folded into FP64 every kFfFoldRows rows.  A value outside [2^-50, 2^59) that is not zero
 // (nor an FP64 subnormal, taken as zero) reports false, and the caller forms that row's
 // product in FP64 instead: every float-pair product and its rounding error then stay
-// normal floats.
-constexpr int kFfFoldRows = 32;
+// normal floats, and a component's sum of 2 kFfFoldRows products stays below 2^126, so the
+// folds (DADDs and conversions on the FP64 pipe, the bound of this step) come every 128 rows.
+constexpr int kFfFoldRows = 128;
 
 __device__ __forceinline__ bool ff_split_f64(double x, float& hi, float& lo) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
@@ -108,15 +109,15 @@ __device__ __forceinline__ bool ff_split_f64(double x, float& hi, float& lo) {
   const float fh = __fsub_rn(__uint_as_float(ch + (unsigned)(d >> 14)), __uint_as_float(ch));
   const float fl = __fsub_rn(__uint_as_float(cl + (unsigned)(d & 0x3fff)), __uint_as_float(cl));
   lo = normal ? __uint_as_float(__float_as_uint(__fadd_rn(fh, fl)) ^ sgn) : 0.f;
-  return e == 0u || (normal && e <= 1083u);
+  return e == 0u || (normal && e <= 1081u);
 }
 
-// a packed left-vector high part: zero, or a normal float in [2^-50, 2^61) (NaN marks an
+// a packed left-vector high part: zero, or a normal float in [2^-50, 2^59) (NaN marks an
 // element that pack_left_ff could not carry)
 __device__ __forceinline__ bool ff_left_ok(float h) {
   const unsigned u = __float_as_uint(h) & 0x7fffffffu;
   const unsigned ef = u >> 23;
-  return u == 0u || (ef >= 77u && ef <= 187u);
+  return u == 0u || (ef >= 77u && ef <= 185u);
 }
 
 // the float pairs of a packed left-vector entry carried in a double2 slot

@@ -128,8 +128,8 @@ __global__ void __launch_bounds__(kWsThreads, (U == 1 ? ((sizeof(T) == 8 && REAL
       tc.vl = static_cast<const unsigned char*>(SER ? p.series : p.vl);
       tc.vl2 = nullptr;
       // complex128: T_m's rows of each staged tile are prefetched into L2 (1.096 -> 1.063 ms per
-      // default step at 2048^2, R = 8), where the tile's neighbour gathers find them; the
-      // complex64 steps measured slower with it (batched ensemble 978 -> 1001 ms)
+      // default step at 2048^2, R = 8), where the tile's neighbour gathers find them; for the
+      // complex64 steps no gain above the spread between GPUs was measured, so they go without
       tc.cur = sizeof(T) == 8 ? static_cast<const unsigned char*>(p.tcur) : nullptr;
       tc.ld = p.ld;
       tc.L = L;

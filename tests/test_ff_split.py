@@ -53,3 +53,20 @@ def test_split_edges():
     assert ok.tolist() == [True, True, True, True, False, False, True, True, False, False, False, False, False]
     assert np.all(hi[:4] == 0) and np.all(lo[:4] == 0)
     assert hi[6] == np.float32(2.0 ** -50) and lo[6] == 0
+
+
+def test_fold_interval_keeps_float_pair_sums_finite():
+    """The float-pair moment sums of the complex128 step are folded into FP64 every kFfFoldRows rows;
+    each component adds two products per row, each below (2^upper)^2 for split inputs below 2^upper.
+    The constants are read from the kernel header, so a longer fold interval without a tighter range
+    (or the reverse) fails here before any float-pair sum can overflow."""
+    import os
+    import re
+
+    src = open(os.path.join(os.path.dirname(__file__), "..", "minijclsquant_gb300", "csrc", "kpm_ff.cuh")).read()
+    rows = int(re.search(r"constexpr int kFfFoldRows = (\d+);", src).group(1))
+    e_max = int(re.search(r"normal && e <= (\d+)u", src).group(1))  # FP64 exponent field of the largest split
+    ef_max = int(re.search(r"ef >= 77u && ef <= (\d+)u", src).group(1))  # float exponent field, left vector
+    upper = e_max - 1023 + 1  # split values are below 2^upper
+    assert ef_max - 127 + 1 == upper  # the left vector's guard matches the split's
+    assert 2 * rows * 2.0 ** (2 * upper) < 2.0 ** 128  # below FLT_MAX's binade

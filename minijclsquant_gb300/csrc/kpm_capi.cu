@@ -178,14 +178,15 @@ int step_config(kpm_ell_s* h, bool f32, int Rg, int sets, cudaStream_t s, StepCo
   // the staged kernel serves one moment set; two-set calls use the grid-stride kernel;
   // doubled moments (sets == 3) and series steps (sets == 4) the grid-stride and the
   // producer-warp kernels
+  // (rows per thread, sub-tiles per stage) of the staged forms; two sub-tiles per stage exist
+  // for the complex128 producer-warp kernel only
+  static const int kForms[][2] = {{1, 1}, {2, 1}, {1, 2}};
   for (int kind = 1; kind <= 2 && sets != 2; ++kind)
-    for (int U = 1; U <= 3; ++U) {
-      // U = 3 stands for one row per thread with two sub-tiles per stage (producer-warp, complex128)
-      const int sb = U == 3 ? 2 : 1;
-      const int u = U == 3 ? 1 : U;
-      if (U == 3 && (kind == 1 || f32)) continue;
+    for (const auto& form : kForms) {
+      const int u = form[0], sb = form[1];
+      if (sb == 2 && (kind == 1 || f32)) continue;
       if ((sets == 3 || sets == 4) && kind == 1) continue;
-      const std::string name = std::string(kind == 1 ? "staged" : "ws") + (U == 2 ? "2" : "1") + (sb == 2 ? "s2" : "");
+      const std::string name = std::string(kind == 1 ? "staged" : "ws") + (u == 2 ? "2" : "1") + (sb == 2 ? "s2" : "");
       if (!f.empty() && f != name) continue;
       const int occ = kind == 1 ? (f32 ? staged_ctas_f32(h->is_real, Rg, u, h->L, 2)
                                        : staged_ctas_f64(h->is_real, Rg, u, h->L, 2))
